@@ -1,0 +1,793 @@
+// crgpu_api.cu - the C ABI of include/crgpu.h: contexts, graph parsing, the v1 solve
+// schedule, verdict, table read-out and the table-file writer.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/crgpu.h"
+#include "crgpu_internal.cuh"
+#include "crgpu_v2.h"
+
+namespace crgpu {
+void launch_cop(const V1Dev& d, int col, int nx, int direct, int grid, cudaStream_t st);
+void launch_and(const V1Dev& d, int col, bool p1, int grid, cudaStream_t st);
+void launch_prep(const V1Dev& d, int col, int nx, int grid, cudaStream_t st);
+void launch_init(const V1Dev& d, int grid, cudaStream_t st);
+void launch_verdict(const V1Dev& d, int cols, unsigned long long* best, int grid, cudaStream_t st);
+void launch_popcount(const uint32_t* plane, size_t words, unsigned long long* out, int grid,
+                     cudaStream_t st);
+int max_cop_blocks_per_sm(int k, int rwp, int S);
+size_t cop_smem_bytes(int S, int rwp);
+size_t and_smem_bytes(int S, int rwp, int n);
+void launch_unrank(const uint32_t* B, int n, int k, uint32_t C, uint16_t* out, int grid, cudaStream_t st);
+int trans_cap(int k, int maxdeg);
+void launch_trans(int k, const uint16_t* configs, uint32_t C, int n, const uint32_t* rp,
+                  const uint16_t* adj, const uint32_t* B, int cap, unsigned long long* counts,
+                  const unsigned long long* heads, unsigned long long* data, unsigned int* err,
+                  int grid, cudaStream_t st);
+void launch_scan(const unsigned long long* in, unsigned long long* out, uint32_t C, cudaStream_t st);
+}  // namespace crgpu
+
+using namespace crgpu;
+
+struct cr_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int num_sms = 1;
+    bool profiling = false;
+    std::string err;
+};
+
+// Per-solve state.  Host copies of the graph are kept for the hop masks and file output.
+struct cr_solver {
+    cr_context* ctx = nullptr;
+    int n = 0, k = 0, p = 0, rules = CR_RULES_V1, cols = 0, rw = 0, rwp = 0, S = 2;
+    uint64_t C = 0;
+    int maxdeg = 0;
+    std::vector<uint32_t> h_rp;
+    std::vector<uint16_t> h_col;
+    std::vector<uint32_t> h_binom;
+    // device
+    uint32_t* d_rp = nullptr;
+    uint16_t* d_col = nullptr;
+    uint32_t* d_binom = nullptr;
+    uint16_t* d_configs = nullptr;
+    uint32_t* d_hop = nullptr;
+    uint8_t* d_table = nullptr;
+    uint32_t* d_marked = nullptr;
+    uint32_t* d_front = nullptr;
+    uint8_t* d_fflag = nullptr;
+    ColMeta* d_meta = nullptr;
+    unsigned long long* d_counters = nullptr;  // [0] pass_new, [1] verdict key, [2] scratch
+    unsigned int* d_err = nullptr;
+    unsigned long long* d_heads = nullptr;
+    unsigned long long* d_trans = nullptr;
+    uint64_t n_trans = 0;
+    unsigned long long* h_pinned = nullptr;  // pinned read-back slot for the pass counter
+    cudaGraphExec_t pass_graph = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evc0 = nullptr, evc1 = nullptr;
+    // phase state
+    bool initialized = false;
+    bool finished = false;
+    uint64_t base_caps = 0;
+    std::vector<uint64_t> pass_counts;
+    cr_solve_stats stats{};
+    int grid_cop = 1, grid_small = 1;
+    crgpu::V2Solver* v2 = nullptr;
+};
+
+static int fail(cr_context* ctx, int code, const char* fmt, ...) {
+    if (ctx) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof(buf), fmt, ap);
+        va_end(ap);
+        ctx->err = buf;
+    }
+    return code;
+}
+
+#define CR_CUDA(ctx, call)                                                                  \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess)                                                              \
+            return fail((ctx), CR_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+static uint64_t binom_u64(int64_t n, int64_t k) {
+    if (k < 0 || n < 0 || k > n) return 0;
+    if (k > n - k) k = n - k;
+    unsigned __int128 r = 1;
+    for (int64_t i = 1; i <= k; ++i) {
+        r = r * (unsigned __int128)(n - i + 1) / (unsigned __int128)i;
+        if (r > (unsigned __int128)UINT64_MAX) return UINT64_MAX;
+    }
+    return (uint64_t)r;
+}
+
+extern "C" {
+
+int cr_context_create(int32_t device, void* stream, cr_context** out) {
+    if (!out) return CR_ERR_INVALID;
+    *out = nullptr;
+    cr_context* c = new (std::nothrow) cr_context();
+    if (!c) return CR_ERR_NOMEM;
+    c->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) {
+        if (stream) {
+            c->stream = (cudaStream_t)stream;
+        } else {
+            e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+            c->own_stream = true;
+        }
+    }
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (e != cudaSuccess) {
+        delete c;
+        return CR_ERR_CUDA;
+    }
+    *out = c;
+    return CR_OK;
+}
+
+int cr_context_destroy(cr_context* ctx) {
+    if (!ctx) return CR_OK;
+    if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return CR_OK;
+}
+
+const char* cr_context_last_error(const cr_context* ctx) { return ctx ? ctx->err.c_str() : ""; }
+
+int cr_context_set_profiling(cr_context* ctx, int32_t on) {
+    if (!ctx) return CR_ERR_INVALID;
+    ctx->profiling = on != 0;
+    return CR_OK;
+}
+
+int cr_graph_parse(const char* text, size_t len, int32_t* n_out, uint32_t* row_ptr,
+                   uint16_t* col_idx, size_t col_cap, size_t* nnz_out) {
+    // Graph::Graph (lib/src/Graph.cpp:26-70): N = first-line width; '0'/'1' fill row-major;
+    // '\n' advances the row only after a digit; '-' ends the matrix; anything else is skipped.
+    if (!n_out || !nnz_out || (!text && len)) return CR_ERR_INVALID;
+    size_t n = 0;
+    while (n < len && text[n] != '\n' && text[n] != '\r' && text[n] != '-') ++n;
+    if (n > CR_MAX_N) return CR_ERR_LIMIT;
+    *n_out = (int32_t)n;
+    std::vector<uint8_t> m(n * n, 0);
+    size_t row = 0, col = 0;
+    for (size_t i = 0; i < len && n; ++i) {
+        char c = text[i];
+        if (c == '-') break;
+        if (c == '0' || c == '1') {
+            if (row < n && col < n) m[row * n + col] = (uint8_t)(c == '1');
+            ++col;
+        } else if (c == '\n') {
+            if (col > 0) { ++row; col = 0; }
+        }
+    }
+    size_t nnz = 0;
+    for (uint8_t x : m) nnz += x;
+    *nnz_out = nnz;
+    if (!row_ptr) return CR_OK;
+    if (!col_idx && nnz) return CR_ERR_INVALID;
+    if (col_cap < nnz) return CR_ERR_INVALID;
+    size_t e = 0;
+    row_ptr[0] = 0;
+    for (size_t r = 0; r < n; ++r) {
+        for (size_t c = 0; c < n; ++c)
+            if (m[r * n + c]) col_idx[e++] = (uint16_t)c;
+        row_ptr[r + 1] = (uint32_t)e;
+    }
+    return CR_OK;
+}
+
+static int slots_for(int n) { (void)n; return 2; }
+
+static void layout(int n, int k, int p, int rules, int S, uint64_t* C, int* cols, int* rw, int* rwp) {
+    *C = binom_u64((int64_t)n + k - 1, k);
+    *cols = rules == CR_RULES_V2 ? 1 : 2 * p;
+    *rw = (n + 31) / 32;
+    *rwp = round_words(*rw);
+    (void)S;
+}
+
+uint64_t cr_solver_footprint(int32_t n, int32_t k, int32_t p, int32_t rules) {
+    if (n <= 0 || k <= 0 || p <= 0) return 0;
+    if (rules == CR_RULES_V2) return crgpu::v2_footprint(n, k, p);
+    uint64_t C;
+    int cols, rw, rwp;
+    const int S = slots_for(n);
+    layout(n, k, p, rules, S, &C, &cols, &rw, &rwp);
+    uint64_t b = C * (uint64_t)n * cols;                 // table
+    b += (uint64_t)cols * C * rwp * 4;                   // marked
+    b += (uint64_t)cols * C * S * rwp * 4;               // frontiers
+    b += (uint64_t)cols * C;                             // flags
+    b += C * (uint64_t)k * 2;                            // configs
+    b += (uint64_t)n * rwp * 4 + (uint64_t)k * (n + 1) * 4 + (1u << 16);
+    return b;
+}
+
+static void free_v1(cr_solver* s) {
+    if (s->pass_graph) cudaGraphExecDestroy(s->pass_graph);
+    s->pass_graph = nullptr;
+    void* ptrs[] = {s->d_rp, s->d_col, s->d_binom, s->d_configs, s->d_hop, s->d_table,
+                    s->d_marked, s->d_front, s->d_fflag, s->d_meta, s->d_counters, s->d_err,
+                    s->d_heads, s->d_trans};
+    for (void* q : ptrs)
+        if (q) cudaFree(q);
+    s->d_rp = nullptr; s->d_col = nullptr; s->d_binom = nullptr; s->d_configs = nullptr;
+    s->d_hop = nullptr; s->d_table = nullptr; s->d_marked = nullptr; s->d_front = nullptr;
+    s->d_fflag = nullptr; s->d_meta = nullptr; s->d_counters = nullptr; s->d_err = nullptr;
+    s->d_heads = nullptr; s->d_trans = nullptr;
+    if (s->h_pinned) cudaFreeHost(s->h_pinned);
+    s->h_pinned = nullptr;
+    cudaEvent_t evs[] = {s->ev0, s->ev1, s->evc0, s->evc1};
+    for (cudaEvent_t e : evs)
+        if (e) cudaEventDestroy(e);
+    s->ev0 = s->ev1 = s->evc0 = s->evc1 = nullptr;
+}
+
+static V1Dev dev_view(const cr_solver* s) {
+    V1Dev d;
+    d.g.n = s->n;
+    d.g.rw = s->rw;
+    d.g.rwp = s->rwp;
+    d.g.row_ptr = s->d_rp;
+    d.g.col = s->d_col;
+    d.k = s->k;
+    d.cols = s->cols;
+    d.S = s->S;
+    d.C = (uint32_t)s->C;
+    d.binom = s->d_binom;
+    d.configs = s->d_configs;
+    d.hop = s->d_hop;
+    d.table = s->d_table;
+    d.marked = s->d_marked;
+    d.front = s->d_front;
+    d.fflag = s->d_fflag;
+    d.meta = s->d_meta;
+    d.pass_new = s->d_counters;
+    d.err = s->d_err;
+    return d;
+}
+
+// Exact-p-hop vertex sets (k_cops_visibility.cpp:245-262, robber self-edges off).
+static std::vector<uint32_t> hop_masks(const cr_solver* s) {
+    std::vector<uint32_t> hop((size_t)s->n * s->rwp, 0);
+    std::vector<uint8_t> cur(s->n), nxt(s->n);
+    for (int r = 0; r < s->n; ++r) {
+        std::fill(cur.begin(), cur.end(), 0);
+        cur[r] = 1;
+        for (int step = 0; step < s->p; ++step) {
+            std::fill(nxt.begin(), nxt.end(), 0);
+            for (int v = 0; v < s->n; ++v)
+                if (cur[v])
+                    for (uint32_t e = s->h_rp[v]; e < s->h_rp[v + 1]; ++e) nxt[s->h_col[e]] = 1;
+            cur.swap(nxt);
+        }
+        for (int v = 0; v < s->n; ++v)
+            if (cur[v]) hop[(size_t)r * s->rwp + (v >> 5)] |= 1u << (v & 31);
+    }
+    return hop;
+}
+
+static int alloc_v1(cr_solver* s) {
+    cr_context* ctx = s->ctx;
+    const size_t C = s->C;
+    CR_CUDA(ctx, cudaMalloc(&s->d_table, C * s->n * s->cols));
+    CR_CUDA(ctx, cudaMalloc(&s->d_marked, (size_t)s->cols * C * s->rwp * 4));
+    CR_CUDA(ctx, cudaMalloc(&s->d_front, (size_t)s->cols * C * s->S * s->rwp * 4));
+    CR_CUDA(ctx, cudaMalloc(&s->d_fflag, (size_t)s->cols * C));
+    CR_CUDA(ctx, cudaMalloc(&s->d_meta, sizeof(ColMeta) * s->cols));
+    CR_CUDA(ctx, cudaMalloc(&s->d_hop, (size_t)s->n * s->rwp * 4));
+    std::vector<uint32_t> hop = hop_masks(s);
+    CR_CUDA(ctx, cudaMemcpyAsync(s->d_hop, hop.data(), hop.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return CR_OK;
+}
+
+int cr_solver_create(cr_context* ctx, const cr_graph* g, int32_t k, int32_t p, int32_t rules,
+                     cr_solver** out) {
+    if (!ctx || !g || !out) return CR_ERR_INVALID;
+    *out = nullptr;
+    if (g->n <= 0) return fail(ctx, CR_ERR_INVALID, "Graph is empty or failed to load.");
+    if (g->n > CR_MAX_N) return fail(ctx, CR_ERR_LIMIT, "n=%d exceeds %d vertices", g->n, CR_MAX_N);
+    if (k <= 0 || k > CR_MAX_K) return fail(ctx, CR_ERR_LIMIT, "k=%d outside 1..%d", k, CR_MAX_K);
+    if (p <= 0 || p > 63) return fail(ctx, CR_ERR_INVALID, "p=%d outside 1..63", p);
+    if (rules != CR_RULES_V1 && rules != CR_RULES_V2) return fail(ctx, CR_ERR_INVALID, "unknown rules %d", rules);
+    if (!g->row_ptr || (g->row_ptr[g->n] && !g->col_idx)) return fail(ctx, CR_ERR_INVALID, "graph arrays missing");
+    for (int v = 0; v < g->n; ++v)
+        if (g->row_ptr[v + 1] < g->row_ptr[v]) return fail(ctx, CR_ERR_INVALID, "row_ptr not monotone");
+    for (uint32_t e = 0; e < g->row_ptr[g->n]; ++e)
+        if (g->col_idx[e] >= g->n) return fail(ctx, CR_ERR_INVALID, "neighbour index out of range");
+    CR_CUDA(ctx, cudaSetDevice(ctx->device));
+
+    cr_solver* s = new (std::nothrow) cr_solver();
+    if (!s) return fail(ctx, CR_ERR_NOMEM, "host allocation failed");
+    s->ctx = ctx;
+    s->n = g->n;
+    s->k = k;
+    s->p = p;
+    s->rules = rules;
+    s->S = slots_for(g->n);
+    layout(s->n, k, p, rules, s->S, &s->C, &s->cols, &s->rw, &s->rwp);
+    if (s->C == 0 || s->C >= (1ull << 32)) {
+        delete s;
+        return fail(ctx, CR_ERR_LIMIT, "config count C(%d,%d) outside 1..2^32-1", g->n + k - 1, k);
+    }
+    s->h_rp.assign(g->row_ptr, g->row_ptr + g->n + 1);
+    s->h_col.assign(g->col_idx, g->col_idx + g->row_ptr[g->n]);
+    for (int v = 0; v < s->n; ++v) s->maxdeg = std::max<int>(s->maxdeg, s->h_rp[v + 1] - s->h_rp[v]);
+    // B[i][x] = C(n - x + k - 1 - i, k - i)
+    s->h_binom.assign((size_t)k * (s->n + 1), 0);
+    for (int i = 0; i < k; ++i)
+        for (int x = 0; x <= s->n; ++x)
+            s->h_binom[(size_t)i * (s->n + 1) + x] = (uint32_t)binom_u64((int64_t)s->n - x + k - 1 - i, k - i);
+
+    auto bail = [&](int code) {
+        free_v1(s);
+        if (s->v2) crgpu::v2_destroy(s->v2);
+        delete s;
+        return code;
+    };
+#define CR_TRY(call)                                                                         \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess) {                                                             \
+            fail(ctx, e_ == cudaErrorMemoryAllocation ? CR_ERR_NOMEM : CR_ERR_CUDA, "%s: %s", \
+                 #call, cudaGetErrorString(e_));                                             \
+            return bail(e_ == cudaErrorMemoryAllocation ? CR_ERR_NOMEM : CR_ERR_CUDA);       \
+        }                                                                                    \
+    } while (0)
+    CR_TRY(cudaMalloc(&s->d_rp, s->h_rp.size() * 4));
+    CR_TRY(cudaMalloc(&s->d_col, std::max<size_t>(s->h_col.size(), 1) * 2));
+    CR_TRY(cudaMalloc(&s->d_binom, s->h_binom.size() * 4));
+    CR_TRY(cudaMalloc(&s->d_configs, s->C * k * 2));
+    CR_TRY(cudaMalloc(&s->d_counters, 4 * sizeof(unsigned long long)));
+    CR_TRY(cudaMalloc(&s->d_err, sizeof(unsigned int)));
+    CR_TRY(cudaMallocHost(&s->h_pinned, 4 * sizeof(unsigned long long)));
+    CR_TRY(cudaEventCreate(&s->ev0));
+    CR_TRY(cudaEventCreate(&s->ev1));
+    CR_TRY(cudaEventCreate(&s->evc0));
+    CR_TRY(cudaEventCreate(&s->evc1));
+    CR_TRY(cudaMemcpyAsync(s->d_rp, s->h_rp.data(), s->h_rp.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+    if (!s->h_col.empty())
+        CR_TRY(cudaMemcpyAsync(s->d_col, s->h_col.data(), s->h_col.size() * 2, cudaMemcpyHostToDevice, ctx->stream));
+    CR_TRY(cudaMemcpyAsync(s->d_binom, s->h_binom.data(), s->h_binom.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CR_TRY(cudaMemsetAsync(s->d_err, 0, sizeof(unsigned int), ctx->stream));
+    {
+        const int grid = (int)std::min<uint64_t>((s->C + 255) / 256, (uint64_t)ctx->num_sms * 8);
+        launch_unrank(s->d_binom, s->n, k, (uint32_t)s->C, s->d_configs, std::max(grid, 1), ctx->stream);
+        CR_TRY(cudaGetLastError());
+    }
+    if (rules == CR_RULES_V1) {
+        if ((uint64_t)s->S * s->rwp / std::min(s->rwp, 4) > 32)
+            return (fail(ctx, CR_ERR_LIMIT, "row too wide for the warp layout"), bail(CR_ERR_LIMIT));
+        int rc = alloc_v1(s);
+        if (rc) return bail(rc);
+        const int per_sm = max_cop_blocks_per_sm(k, s->rwp, s->S);
+        s->grid_cop = (int)std::max<uint64_t>(1, std::min<uint64_t>((s->C + 7) / 8, (uint64_t)ctx->num_sms * per_sm));
+        s->grid_small = (int)std::max<uint64_t>(1, std::min<uint64_t>((s->C + 255) / 256, (uint64_t)ctx->num_sms * 4));
+        if (and_smem_bytes(s->S, s->rwp, s->n) > 48 * 1024 || cop_smem_bytes(s->S, s->rwp) > 48 * 1024)
+            return (fail(ctx, CR_ERR_LIMIT, "shared memory layout too large"), bail(CR_ERR_LIMIT));
+    } else {
+        int rc = crgpu::v2_create(&s->v2, ctx->stream, ctx->num_sms, s->n, k, p, s->d_rp, s->d_col,
+                                  s->h_rp.data(), s->h_col.data(), s->d_binom, s->d_configs,
+                                  (uint32_t)s->C, &ctx->err);
+        if (rc) return bail(rc);
+    }
+    CR_TRY(cudaStreamSynchronize(ctx->stream));
+#undef CR_TRY
+    s->stats.slots = s->S;
+    *out = s;
+    return CR_OK;
+}
+
+int cr_solver_destroy(cr_solver* s) {
+    if (!s) return CR_OK;
+    cudaSetDevice(s->ctx->device);
+    free_v1(s);
+    if (s->v2) crgpu::v2_destroy(s->v2);
+    delete s;
+    return CR_OK;
+}
+
+static int check_err(cr_solver* s, unsigned* bits) {
+    cr_context* ctx = s->ctx;
+    unsigned e = 0;
+    CR_CUDA(ctx, cudaMemcpyAsync(&e, s->d_err, sizeof(e), cudaMemcpyDeviceToHost, ctx->stream));
+    CR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    *bits = e;
+    return CR_OK;
+}
+
+// v1 initializeCaptures on the device.
+static int v1_init(cr_solver* s, uint64_t* caps) {
+    cr_context* ctx = s->ctx;
+    cudaStream_t st = ctx->stream;
+    const size_t C = s->C;
+    CR_CUDA(ctx, cudaEventRecord(s->ev0, st));
+    CR_CUDA(ctx, cudaMemsetAsync(s->d_table, kUnmarked, C * s->n * s->cols, st));
+    CR_CUDA(ctx, cudaMemsetAsync(s->d_marked, 0, (size_t)s->cols * C * s->rwp * 4, st));
+    CR_CUDA(ctx, cudaMemsetAsync(s->d_front, 0, (size_t)2 * C * s->S * s->rwp * 4, st));
+    CR_CUDA(ctx, cudaMemsetAsync(s->d_fflag, 0, (size_t)s->cols * C, st));
+    CR_CUDA(ctx, cudaMemsetAsync(s->d_counters, 0, 4 * sizeof(unsigned long long), st));
+    CR_CUDA(ctx, cudaMemsetAsync(s->d_err, 0, sizeof(unsigned), st));
+    std::vector<ColMeta> meta(s->cols);
+    for (int c = 0; c < s->cols; ++c) meta[c] = ColMeta{0, kEmptyLo, -1, 0};
+    meta[0] = ColMeta{0, 0, 0, 1};  // capture seeds; pass 1's column-0 producer appends to them
+    meta[1] = ColMeta{0, 0, 0, 0};
+    CR_CUDA(ctx, cudaMemcpyAsync(s->d_meta, meta.data(), sizeof(ColMeta) * s->cols, cudaMemcpyHostToDevice, st));
+    V1Dev d = dev_view(s);
+    launch_init(d, s->grid_small, st);
+    CR_CUDA(ctx, cudaGetLastError());
+    CR_CUDA(ctx, cudaEventRecord(s->ev1, st));
+    CR_CUDA(ctx, cudaMemcpyAsync(s->h_pinned, s->d_counters, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    CR_CUDA(ctx, cudaStreamSynchronize(st));
+    *caps = s->h_pinned[0];
+    float ms = 0;
+    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+    s->stats.init_ms = ms;
+    s->stats.kernel_launches = 1;
+    return CR_OK;
+}
+
+// Enqueue one pass: per column a prep kernel and its producer, then the pass counter copy.
+static int v1_enqueue_pass(cr_solver* s, bool profile) {
+    cr_context* ctx = s->ctx;
+    cudaStream_t st = ctx->stream;
+    V1Dev d = dev_view(s);
+    for (int col = 0; col < s->cols; ++col) {
+        const int nx = (col + 1) % s->cols;
+        launch_prep(d, col, nx, s->grid_small, st);
+        if (col % 2 == 0) {
+            if (profile) CR_CUDA(ctx, cudaEventRecord(s->evc0, st));
+            launch_cop(d, col, nx, 0, s->grid_cop, st);
+            if (profile) CR_CUDA(ctx, cudaEventRecord(s->evc1, st));
+        } else if (col < s->cols - 1) {
+            launch_cop(d, col, nx, 1, s->grid_cop, st);
+        } else {
+            launch_and(d, col, s->p == 1, s->grid_cop, st);
+        }
+        CR_CUDA(ctx, cudaGetLastError());
+        if (profile && col % 2 == 0) {
+            // per-launch timing of the cop turn (the dominant kernel)
+            CR_CUDA(ctx, cudaEventSynchronize(s->evc1));
+            float ms = 0;
+            cudaEventElapsedTime(&ms, s->evc0, s->evc1);
+            s->stats.cop_step_ms += ms;
+            s->stats.cop_step_launches += 1;
+        }
+    }
+    CR_CUDA(ctx, cudaMemcpyAsync(s->h_pinned, s->d_counters, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    return CR_OK;
+}
+
+static int v1_pass(cr_solver* s, uint64_t* found) {
+    cr_context* ctx = s->ctx;
+    cudaStream_t st = ctx->stream;
+    if (ctx->profiling) {
+        int rc = v1_enqueue_pass(s, true);
+        if (rc) return rc;
+    } else {
+        if (!s->pass_graph) {
+            cudaGraph_t graph;
+            CR_CUDA(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            int rc = v1_enqueue_pass(s, false);
+            cudaError_t e = cudaStreamEndCapture(st, &graph);
+            if (rc) return rc;
+            if (e != cudaSuccess) return fail(ctx, CR_ERR_CUDA, "pass capture: %s", cudaGetErrorString(e));
+            e = cudaGraphInstantiate(&s->pass_graph, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) return fail(ctx, CR_ERR_CUDA, "pass graph: %s", cudaGetErrorString(e));
+        }
+        CR_CUDA(ctx, cudaGraphLaunch(s->pass_graph, st));
+    }
+    CR_CUDA(ctx, cudaStreamSynchronize(st));
+    s->stats.kernel_launches += 2 * s->cols;
+    *found = s->h_pinned[0];
+    return CR_OK;
+}
+
+int cr_solver_init(cr_solver* s, uint64_t* base_captures) {
+    if (!s) return CR_ERR_INVALID;
+    cr_context* ctx = s->ctx;
+    CR_CUDA(ctx, cudaSetDevice(ctx->device));
+    uint64_t caps = 0;
+    int rc = s->rules == CR_RULES_V1 ? v1_init(s, &caps) : crgpu::v2_init(s->v2, &caps, &s->stats, &ctx->err);
+    if (rc) return rc;
+    s->base_caps = caps;
+    s->pass_counts.clear();
+    s->initialized = true;
+    s->finished = false;
+    s->stats.main_ms = 0;
+    s->stats.cop_step_ms = 0;
+    s->stats.cop_step_launches = 0;
+    s->stats.passes = 0;
+    if (base_captures) *base_captures = caps;
+    return CR_OK;
+}
+
+static int grow_slots_and_replay(cr_solver* s) {
+    // A frontier needed more value slots than allocated: widen and replay from the start.
+    cr_context* ctx = s->ctx;
+    if (s->S >= 8) return fail(ctx, CR_ERR_INTERNAL, "frontier value range exceeds 8 slots");
+    std::vector<uint64_t> done = s->pass_counts;
+    cudaFree(s->d_front);
+    s->d_front = nullptr;
+    if (s->pass_graph) cudaGraphExecDestroy(s->pass_graph);
+    s->pass_graph = nullptr;
+    s->S *= 2;
+    if ((uint64_t)s->S * s->rwp / std::min(s->rwp, 4) > 32)
+        return fail(ctx, CR_ERR_LIMIT, "row too wide for %d value slots", s->S);
+    CR_CUDA(ctx, cudaMalloc(&s->d_front, (size_t)s->cols * s->C * s->S * s->rwp * 4));
+    const int per_sm = max_cop_blocks_per_sm(s->k, s->rwp, s->S);
+    s->grid_cop = (int)std::max<uint64_t>(1, std::min<uint64_t>((s->C + 7) / 8, (uint64_t)ctx->num_sms * per_sm));
+    uint64_t caps;
+    int rc = v1_init(s, &caps);
+    if (rc) return rc;
+    s->stats.slots = s->S;
+    for (size_t i = 0; i < done.size(); ++i) {
+        uint64_t f;
+        rc = v1_pass(s, &f);
+        if (rc) return rc;
+        if (f != done[i]) return fail(ctx, CR_ERR_INTERNAL, "replay diverged at pass %zu", i + 1);
+    }
+    return CR_OK;
+}
+
+int cr_solver_pass(cr_solver* s, uint64_t* new_wins) {
+    if (!s || !new_wins) return CR_ERR_INVALID;
+    cr_context* ctx = s->ctx;
+    if (!s->initialized) return fail(ctx, CR_ERR_STATE, "initializeCaptures has not run");
+    if (s->finished) { *new_wins = 0; return CR_OK; }
+    CR_CUDA(ctx, cudaSetDevice(ctx->device));
+    uint64_t f = 0;
+    if (s->rules == CR_RULES_V2) {
+        int rc = crgpu::v2_pass(s->v2, &f, &s->stats, &ctx->err);
+        if (rc) return rc;
+    } else {
+        for (int attempt = 0;; ++attempt) {
+            CR_CUDA(ctx, cudaEventRecord(s->ev0, ctx->stream));
+            int rc = v1_pass(s, &f);
+            if (rc) return rc;
+            CR_CUDA(ctx, cudaEventRecord(s->ev1, ctx->stream));
+            CR_CUDA(ctx, cudaEventSynchronize(s->ev1));
+            float ms = 0;
+            cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+            s->stats.main_ms += ms;
+            unsigned bits = 0;
+            rc = check_err(s, &bits);
+            if (rc) return rc;
+            if (bits & kErrRank) return fail(ctx, CR_ERR_INTERNAL, "successor rank out of range");
+            if (!(bits & kErrSlot)) break;
+            if (attempt > 3) return fail(ctx, CR_ERR_INTERNAL, "value slots kept overflowing");
+            rc = grow_slots_and_replay(s);
+            if (rc) return rc;
+        }
+    }
+    s->pass_counts.push_back(f);
+    s->stats.passes = (int)s->pass_counts.size();
+    if (f == 0) s->finished = true;
+    *new_wins = f;
+    return CR_OK;
+}
+
+int cr_solver_run(cr_solver* s, uint64_t* pass_counts, int32_t cap, int32_t* passes) {
+    if (!s) return CR_ERR_INVALID;
+    for (int i = 0; i < 1 << 16; ++i) {
+        uint64_t f;
+        int rc = cr_solver_pass(s, &f);
+        if (rc) return rc;
+        if (s->finished) break;
+    }
+    if (!s->finished) return fail(s->ctx, CR_ERR_BUDGET, "no fixed point after 65536 passes");
+    if (passes) *passes = (int32_t)s->pass_counts.size();
+    if (pass_counts)
+        for (size_t i = 0; i < s->pass_counts.size() && (int32_t)i < cap; ++i) pass_counts[i] = s->pass_counts[i];
+    return CR_OK;
+}
+
+int cr_solver_verdict(cr_solver* s, cr_verdict* out) {
+    if (!s || !out) return CR_ERR_INVALID;
+    cr_context* ctx = s->ctx;
+    CR_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    const unsigned long long init = ~0ull;
+    CR_CUDA(ctx, cudaMemcpyAsync(s->d_counters + 1, &init, sizeof(init), cudaMemcpyHostToDevice, st));
+    if (s->rules == CR_RULES_V1) {
+        V1Dev d = dev_view(s);
+        launch_verdict(d, s->cols, s->d_counters + 1, s->grid_cop, st);
+    } else {
+        crgpu::v2_verdict(s->v2, s->d_counters + 1);
+    }
+    CR_CUDA(ctx, cudaGetLastError());
+    CR_CUDA(ctx, cudaMemcpyAsync(s->h_pinned + 1, s->d_counters + 1, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    CR_CUDA(ctx, cudaStreamSynchronize(st));
+    const unsigned long long key = s->h_pinned[1];
+    memset(out, 0, sizeof(*out));
+    if (key == ~0ull || (int)(key >> 32) >= kMaxRound) {
+        out->win = 0;
+        out->best_config = -1;
+        out->capture_plies = kMaxRound;
+        return CR_OK;
+    }
+    out->win = 1;
+    out->best_config = (int64_t)(key & 0xFFFFFFFFull);
+    out->capture_plies = (int32_t)(key >> 32);
+    uint16_t pos[CR_MAX_K];
+    CR_CUDA(ctx, cudaMemcpyAsync(pos, s->d_configs + (size_t)out->best_config * s->k, s->k * 2, cudaMemcpyDeviceToHost, st));
+    CR_CUDA(ctx, cudaStreamSynchronize(st));
+    for (int i = 0; i < s->k; ++i) out->positions[i] = pos[i];
+    return CR_OK;
+}
+
+int cr_solver_sizes(cr_solver* s, cr_table_sizes* out) {
+    if (!s || !out) return CR_ERR_INVALID;
+    out->config_count = s->C;
+    out->columns = s->cols;
+    out->num_states = s->C * (uint64_t)s->n * s->cols;
+    out->k = s->k;
+    out->n = s->n;
+    out->pad = 0;
+    out->transitions = s->n_trans;
+    return CR_OK;
+}
+
+int cr_solver_stats(cr_solver* s, cr_solve_stats* out) {
+    if (!s || !out) return CR_ERR_INVALID;
+    *out = s->stats;
+    uint64_t res = s->base_caps * (s->rules == CR_RULES_V1 ? 2 : 1);
+    for (uint64_t c : s->pass_counts) res += c;
+    out->resolved = res;
+    return CR_OK;
+}
+
+static const uint8_t* table_ptr(const cr_solver* s) {
+    return s->rules == CR_RULES_V1 ? s->d_table : crgpu::v2_table(s->v2);
+}
+
+int cr_solver_device_states(cr_solver* s, void** dev_ptr, size_t* bytes) {
+    if (!s || !dev_ptr || !bytes) return CR_ERR_INVALID;
+    *dev_ptr = (void*)table_ptr(s);
+    *bytes = s->C * (size_t)s->n * s->cols;
+    return CR_OK;
+}
+
+int cr_solver_read_states(cr_solver* s, uint8_t* dst, size_t bytes) {
+    if (!s || !dst) return CR_ERR_INVALID;
+    cr_context* ctx = s->ctx;
+    const size_t need = s->C * (size_t)s->n * s->cols;
+    if (bytes < need) return fail(ctx, CR_ERR_INVALID, "states buffer holds %zu of %zu bytes", bytes, need);
+    CR_CUDA(ctx, cudaSetDevice(ctx->device));
+    CR_CUDA(ctx, cudaMemcpyAsync(dst, table_ptr(s), need, cudaMemcpyDeviceToHost, ctx->stream));
+    CR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return CR_OK;
+}
+
+int cr_solver_read_configs(cr_solver* s, uint8_t* dst, size_t bytes) {
+    if (!s || !dst) return CR_ERR_INVALID;
+    cr_context* ctx = s->ctx;
+    if (s->n > 256) return fail(ctx, CR_ERR_LIMIT, "the table file stores vertices as uint8 (n <= 256)");
+    const size_t cnt = s->C * (size_t)s->k;
+    if (bytes < cnt) return fail(ctx, CR_ERR_INVALID, "configs buffer too small");
+    std::vector<uint16_t> h(cnt);
+    CR_CUDA(ctx, cudaMemcpyAsync(h.data(), s->d_configs, cnt * 2, cudaMemcpyDeviceToHost, ctx->stream));
+    CR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (size_t i = 0; i < cnt; ++i) dst[i] = (uint8_t)h[i];
+    return CR_OK;
+}
+
+int cr_solver_build_transitions(cr_solver* s, uint64_t* total) {
+    if (!s) return CR_ERR_INVALID;
+    cr_context* ctx = s->ctx;
+    CR_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    if (!s->d_heads) {
+        const int cap = trans_cap(s->k, s->maxdeg);
+        if (cap > 8192) return fail(ctx, CR_ERR_LIMIT, "successor fan-out %d too large for the CSR builder", cap);
+        unsigned long long* counts = nullptr;
+        CR_CUDA(ctx, cudaMalloc(&counts, s->C * 8));
+        CR_CUDA(ctx, cudaMalloc(&s->d_heads, (s->C + 1) * 8));
+        CR_CUDA(ctx, cudaMemsetAsync(s->d_err, 0, sizeof(unsigned), st));
+        const int grid = ctx->num_sms * 8;
+        launch_trans(s->k, s->d_configs, (uint32_t)s->C, s->n, s->d_rp, s->d_col, s->d_binom, cap, counts,
+                     nullptr, nullptr, s->d_err, grid, st);
+        launch_scan(counts, s->d_heads, (uint32_t)s->C, st);
+        CR_CUDA(ctx, cudaGetLastError());
+        unsigned long long tot = 0;
+        CR_CUDA(ctx, cudaMemcpyAsync(&tot, s->d_heads + s->C, 8, cudaMemcpyDeviceToHost, st));
+        CR_CUDA(ctx, cudaStreamSynchronize(st));
+        cudaFree(counts);
+        s->n_trans = tot;
+        CR_CUDA(ctx, cudaMalloc(&s->d_trans, std::max<uint64_t>(tot, 1) * 8));
+        launch_trans(s->k, s->d_configs, (uint32_t)s->C, s->n, s->d_rp, s->d_col, s->d_binom, cap, nullptr,
+                     s->d_heads, s->d_trans, s->d_err, grid, st);
+        CR_CUDA(ctx, cudaGetLastError());
+        unsigned bits = 0;
+        int rc = check_err(s, &bits);
+        if (rc) return rc;
+        if (bits) return fail(ctx, CR_ERR_LIMIT, "successor fan-out exceeded the builder's buffer");
+    }
+    if (total) *total = s->n_trans;
+    return CR_OK;
+}
+
+int cr_solver_read_transitions(cr_solver* s, uint64_t* heads, size_t heads_len, uint64_t* data,
+                               size_t data_len) {
+    if (!s) return CR_ERR_INVALID;
+    cr_context* ctx = s->ctx;
+    int rc = cr_solver_build_transitions(s, nullptr);
+    if (rc) return rc;
+    if (heads) {
+        if (heads_len < s->C + 1) return fail(ctx, CR_ERR_INVALID, "heads buffer too small");
+        CR_CUDA(ctx, cudaMemcpyAsync(heads, s->d_heads, (s->C + 1) * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    if (data) {
+        if (data_len < s->n_trans) return fail(ctx, CR_ERR_INVALID, "transitions buffer too small");
+        if (s->n_trans) CR_CUDA(ctx, cudaMemcpyAsync(data, s->d_trans, s->n_trans * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    CR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return CR_OK;
+}
+
+int cr_solver_write_table_file(cr_solver* s, const char* path) {
+    // CacheManager::saveAuxGraph (lib/include/CacheManager.h:28-75): 12 x u64 header
+    // (k, N, columns, configCount, numStates, sizeof(T)=1, copSelf=0, robberSelf=0, four
+    // section offsets), then configs u8, heads u64, transitions u64, states.
+    if (!s || !path) return CR_ERR_INVALID;
+    cr_context* ctx = s->ctx;
+    int rc = cr_solver_build_transitions(s, nullptr);
+    if (rc) return rc;
+    const uint64_t cfg = s->C * (uint64_t)s->k, heads = (s->C + 1) * 8, trans = s->n_trans * 8;
+    const uint64_t states = s->C * (uint64_t)s->n * s->cols;
+    uint64_t hdr[12] = {(uint64_t)s->k, (uint64_t)s->n, (uint64_t)s->cols, s->C, states, 1, 0, 0,
+                        96, 96 + cfg, 96 + cfg + heads, 96 + cfg + heads + trans};
+    FILE* f = fopen(path, "wb");
+    if (!f) return fail(ctx, CR_ERR_IO, "cannot open %s for writing", path);
+    std::vector<uint8_t> buf;
+    bool ok = fwrite(hdr, 1, 96, f) == 96;
+    buf.resize(cfg);
+    rc = cr_solver_read_configs(s, buf.data(), buf.size());
+    if (rc) { fclose(f); return rc; }
+    ok = ok && fwrite(buf.data(), 1, cfg, f) == cfg;
+    std::vector<uint64_t> hv(s->C + 1), tv(std::max<uint64_t>(s->n_trans, 1));
+    rc = cr_solver_read_transitions(s, hv.data(), hv.size(), tv.data(), tv.size());
+    if (rc) { fclose(f); return rc; }
+    ok = ok && fwrite(hv.data(), 1, heads, f) == heads;
+    ok = ok && (trans == 0 || fwrite(tv.data(), 1, trans, f) == trans);
+    buf.resize(states);
+    rc = cr_solver_read_states(s, buf.data(), buf.size());
+    if (rc) { fclose(f); return rc; }
+    ok = ok && fwrite(buf.data(), 1, states, f) == states;
+    ok = (fclose(f) == 0) && ok;
+    if (!ok) return fail(ctx, CR_ERR_IO, "short write to %s", path);
+    return CR_OK;
+}
+
+int cr_solve(cr_context* ctx, const cr_graph* g, int32_t k, int32_t p, int32_t rules,
+             uint8_t* states_out, size_t states_bytes, uint64_t* pass_counts, int32_t cap,
+             int32_t* passes, cr_verdict* verdict, cr_solve_stats* stats) {
+    cr_solver* s = nullptr;
+    int rc = cr_solver_create(ctx, g, k, p, rules, &s);
+    if (rc) return rc;
+    rc = cr_solver_init(s, nullptr);
+    if (!rc) rc = cr_solver_run(s, pass_counts, cap, passes);
+    if (!rc && verdict) rc = cr_solver_verdict(s, verdict);
+    if (!rc && states_out) rc = cr_solver_read_states(s, states_out, states_bytes);
+    if (!rc && stats) rc = cr_solver_stats(s, stats);
+    cr_solver_destroy(s);
+    return rc;
+}
+
+}  // extern "C"

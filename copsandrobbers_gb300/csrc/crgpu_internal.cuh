@@ -1,0 +1,108 @@
+// crgpu_internal.cuh - device data layout and helpers shared by the solver kernels.
+//
+// State store (one solve):
+//   table   uint8  [C][n][cols]      the reference's states section, byte = marked | round << 1,
+//                                    0xFE unmarked (solvers/k_cops_visibility.cpp:20-26,
+//                                    index (cId * N + r) * columns + col, AuxGraph.h:96-98)
+//   marked  uint32 [cols][C][rwp]    bit r of row C: state (C, r, col) is marked
+//   front   uint32 [cols][C][S][rwp] marks the column's last producer run made, split by
+//                                    value: slot s holds the states of value base + s
+//   fflag   uint8  [cols][C]         1 = row C of the column's frontier is non-empty
+//   configs uint16 [C][k]            sorted cop multisets in lexicographic order (AuxGraph.h:117-177)
+// rw = ceil(n / 32) words of robber bits per row; rwp pads rw to 1, 2 or a multiple of 4 so
+// that a row starts on a 16-byte boundary and loads as uint4 vectors.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace crgpu {
+
+constexpr int kMaxRound = 127;      // MAX_ROUND_COUNT, k_cops_visibility.cpp:26
+constexpr int kEmptyLo = 1 << 20;   // "no value yet" for frontier ranges
+constexpr uint8_t kUnmarked = 0xFE;
+
+// Device-side error bits (ORed into DevState::err).
+constexpr unsigned kErrSlot = 1u;    // a value fell outside the frontier's value slots
+constexpr unsigned kErrRank = 2u;    // a successor rank fell outside [0, C)
+constexpr unsigned kErrBudget = 4u;  // a bounded device loop ran out
+
+// Range and base of the value slots of one column's frontier.
+struct ColMeta {
+    int base;    // value of slot 0
+    int lo;      // smallest value in the frontier (kEmptyLo when empty)
+    int hi;      // largest value in the frontier (-1 when empty)
+    int append;  // 1 = the next producer run adds to the frontier instead of replacing it
+};
+
+struct DevGraph {
+    int n;
+    int rw;               // 32-bit words per robber row
+    int rwp;              // padded words per row
+    const uint32_t* row_ptr;  // n + 1
+    const uint16_t* col;      // out-neighbours, ascending
+};
+
+// Everything one v1 solve's kernels touch.
+struct V1Dev {
+    DevGraph g;
+    int k, cols, S;
+    uint32_t C;
+    const uint32_t* binom;    // [k][n + 1]: B[i][x] = C(n - x + k - 1 - i, k - i)
+    const uint16_t* configs;  // [C][k]
+    const uint32_t* hop;      // [n][rwp]: vertices exactly p robber moves from r
+    uint8_t* table;
+    uint32_t* marked;
+    uint32_t* front;
+    uint8_t* fflag;
+    ColMeta* meta;            // [cols]
+    unsigned long long* pass_new;
+    unsigned int* err;
+};
+
+__host__ __device__ inline int round_words(int rw) { return rw <= 2 ? rw : (rw + 3) & ~3; }
+
+// Valid robber bits of word w of a row (the tail word of a row is partial).
+__device__ __forceinline__ uint32_t valid_mask(int n, int w) {
+    int lo = w * 32;
+    if (lo >= n) return 0u;
+    int left = n - lo;
+    return left >= 32 ? 0xFFFFFFFFu : ((1u << left) - 1u);
+}
+
+// Lexicographic rank of a sorted multiset c[0..K) (the order of AuxGraph.h:160-176).
+// Counting the multisets below c position by position and summing each position's range by
+// the hockey-stick identity gives rank = sum_i B[i][c_{i-1}] - B[i][c_i] with c_{-1} = 0.
+template <int K>
+__device__ __forceinline__ uint32_t config_rank(const int (&c)[K], const uint32_t* __restrict__ B,
+                                                int np1) {
+    uint32_t r = 0;
+    int prev = 0;
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+        r += __ldg(&B[i * np1 + prev]) - __ldg(&B[i * np1 + c[i]]);
+        prev = c[i];
+    }
+    return r;
+}
+
+template <int K>
+__device__ __forceinline__ void sort_small(int (&c)[K]) {
+#pragma unroll
+    for (int i = 1; i < K; ++i) {
+#pragma unroll
+        for (int j = i; j > 0; --j) {
+            int a = c[j - 1], b = c[j];
+            c[j - 1] = min(a, b);
+            c[j] = max(a, b);
+        }
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_or(T v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v |= __shfl_xor_sync(0xFFFFFFFFu, v, off);
+    return v;
+}
+
+}  // namespace crgpu

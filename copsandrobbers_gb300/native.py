@@ -1,0 +1,128 @@
+"""ctypes binding of libcrgpu.so (the C ABI declared in include/crgpu.h).
+
+The library is the only compute path: if it is missing or fails to load, every entry point
+raises instead of falling back to anything else.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcrgpu.so")
+
+CR_OK = 0
+ERRORS = {
+    1: "CR_ERR_INVALID", 2: "CR_ERR_NOMEM", 3: "CR_ERR_CUDA", 4: "CR_ERR_LIMIT",
+    5: "CR_ERR_INTERNAL", 6: "CR_ERR_BUDGET", 7: "CR_ERR_IO", 8: "CR_ERR_STATE",
+}
+CR_RULES_V1 = 1
+CR_RULES_V2 = 2
+CR_MAX_K = 4
+
+c_u64p = ctypes.POINTER(ctypes.c_uint64)
+c_u32p = ctypes.POINTER(ctypes.c_uint32)
+c_u16p = ctypes.POINTER(ctypes.c_uint16)
+c_u8p = ctypes.POINTER(ctypes.c_uint8)
+c_i32p = ctypes.POINTER(ctypes.c_int32)
+
+
+class CrGraph(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int32), ("row_ptr", c_u32p), ("col_idx", c_u16p)]
+
+
+class CrVerdict(ctypes.Structure):
+    _fields_ = [("win", ctypes.c_int32), ("capture_plies", ctypes.c_int32),
+                ("best_config", ctypes.c_int64), ("positions", ctypes.c_uint16 * CR_MAX_K)]
+
+
+class CrTableSizes(ctypes.Structure):
+    _fields_ = [("config_count", ctypes.c_uint64), ("num_states", ctypes.c_uint64),
+                ("columns", ctypes.c_int32), ("k", ctypes.c_int32), ("n", ctypes.c_int32),
+                ("pad", ctypes.c_int32), ("transitions", ctypes.c_uint64)]
+
+
+class CrSolveStats(ctypes.Structure):
+    _fields_ = [("init_ms", ctypes.c_double), ("main_ms", ctypes.c_double),
+                ("cop_step_ms", ctypes.c_double), ("cop_step_launches", ctypes.c_int64),
+                ("kernel_launches", ctypes.c_int64), ("passes", ctypes.c_int32),
+                ("slots", ctypes.c_int32), ("resolved", ctypes.c_uint64)]
+
+
+class CrBatchJob(ctypes.Structure):
+    _fields_ = [("graph", CrGraph), ("k", ctypes.c_int32), ("p", ctypes.c_int32)]
+
+
+class CrBatchResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("passes", ctypes.c_int32),
+                ("verdict", CrVerdict), ("states", ctypes.c_uint64),
+                ("base_captures", ctypes.c_uint64), ("table_digest", ctypes.c_uint64)]
+
+
+class CrGpuError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {message}")
+        self.code = code
+
+
+# Every symbol include/crgpu.h declares, with (restype, argtypes).
+SIGNATURES = {
+    "cr_context_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
+    "cr_context_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "cr_context_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+    "cr_context_set_profiling": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    "cr_solver_footprint": (ctypes.c_uint64, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
+    "cr_graph_parse": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t, c_i32p, c_u32p, c_u16p,
+                                      ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
+    "cr_solver_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(CrGraph), ctypes.c_int32,
+                                        ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]),
+    "cr_solver_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "cr_solver_init": (ctypes.c_int, [ctypes.c_void_p, c_u64p]),
+    "cr_solver_pass": (ctypes.c_int, [ctypes.c_void_p, c_u64p]),
+    "cr_solver_run": (ctypes.c_int, [ctypes.c_void_p, c_u64p, ctypes.c_int32, c_i32p]),
+    "cr_solver_verdict": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(CrVerdict)]),
+    "cr_solver_sizes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(CrTableSizes)]),
+    "cr_solver_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(CrSolveStats)]),
+    "cr_solver_read_states": (ctypes.c_int, [ctypes.c_void_p, c_u8p, ctypes.c_size_t]),
+    "cr_solver_device_states": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p),
+                                               ctypes.POINTER(ctypes.c_size_t)]),
+    "cr_solver_read_configs": (ctypes.c_int, [ctypes.c_void_p, c_u8p, ctypes.c_size_t]),
+    "cr_solver_build_transitions": (ctypes.c_int, [ctypes.c_void_p, c_u64p]),
+    "cr_solver_read_transitions": (ctypes.c_int, [ctypes.c_void_p, c_u64p, ctypes.c_size_t, c_u64p,
+                                                  ctypes.c_size_t]),
+    "cr_solver_write_table_file": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
+    "cr_solve": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(CrGraph), ctypes.c_int32, ctypes.c_int32,
+                                ctypes.c_int32, c_u8p, ctypes.c_size_t, c_u64p, ctypes.c_int32, c_i32p,
+                                ctypes.POINTER(CrVerdict), ctypes.POINTER(CrSolveStats)]),
+}
+
+_lib = None
+
+
+def lib():
+    """Load libcrgpu.so (raising if it is absent: there is no other compute path)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run __graft_entry__.build() (or python -m "
+                              "copsandrobbers_gb300.build) to compile the CUDA extension")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def declared_symbols() -> list[str]:
+    """Function names declared in include/crgpu.h and include/*.h, parsed from the headers."""
+    import glob
+    import re
+
+    names = []
+    for h in sorted(glob.glob(os.path.join(os.path.dirname(HERE), "include", "*.h"))):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names += re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_]*\s*\*?\s*(cr_[a-z0-9_]+)\s*\(", text, flags=re.M)
+    return sorted(set(names))

@@ -1,0 +1,221 @@
+"""Python host API over the C ABI: contexts, phase-by-phase solvers and whole solves.
+
+The phase methods mirror the reference's solver contract (app/main.cpp:11-16):
+``Solver(...)`` is buildAuxGraph, ``init()`` initializeCaptures, ``run()`` mainLoop,
+``verdict()`` findFinalResult and ``write_table_file()`` outputData.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import native as N
+from .graphs import Graph
+
+
+def _check(ctx_ptr, rc: int):
+    if rc != N.CR_OK:
+        msg = N.lib().cr_context_last_error(ctx_ptr) if ctx_ptr else b""
+        raise N.CrGpuError(rc, (msg or b"").decode(errors="replace"))
+
+
+class Context:
+    """One device and one stream (``stream`` = a cudaStream_t handle as int, or None)."""
+
+    def __init__(self, device: int = 0, stream: int | None = None):
+        self.ptr = ctypes.c_void_p()
+        rc = N.lib().cr_context_create(device, ctypes.c_void_p(stream) if stream else None,
+                                       ctypes.byref(self.ptr))
+        if rc != N.CR_OK:
+            raise N.CrGpuError(rc, "cr_context_create failed (no usable CUDA device?)")
+
+    def set_profiling(self, on: bool) -> None:
+        _check(self.ptr, N.lib().cr_context_set_profiling(self.ptr, int(on)))
+
+    def close(self) -> None:
+        if self.ptr:
+            N.lib().cr_context_destroy(self.ptr)
+            self.ptr = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class _GraphArgs:
+    """Keeps the CSR arrays alive for as long as the C struct points at them."""
+
+    def __init__(self, g: Graph):
+        self.row_ptr, self.col = g.csr()
+        if self.col.size == 0:
+            self.col = np.zeros(1, dtype=np.uint16)
+        self.struct = N.CrGraph(g.n, self.row_ptr.ctypes.data_as(N.c_u32p),
+                                self.col.ctypes.data_as(N.c_u16p))
+
+
+@dataclass
+class Verdict:
+    win: bool
+    capture_plies: int
+    best_config: int
+    positions: tuple = field(default_factory=tuple)
+
+
+def _verdict(v: N.CrVerdict, k: int) -> Verdict:
+    return Verdict(bool(v.win), int(v.capture_plies), int(v.best_config),
+                   tuple(int(v.positions[i]) for i in range(k)) if v.win else ())
+
+
+class Solver:
+    """A device state store for one (graph, k, p, rules) solve."""
+
+    def __init__(self, ctx: Context, graph: Graph, k: int, p: int = 1, rules: int = N.CR_RULES_V1):
+        self.ctx, self.graph, self.k, self.p, self.rules = ctx, graph, k, p, rules
+        self._g = _GraphArgs(graph)
+        self.ptr = ctypes.c_void_p()
+        _check(ctx.ptr, N.lib().cr_solver_create(ctx.ptr, ctypes.byref(self._g.struct), k, p, rules,
+                                                 ctypes.byref(self.ptr)))
+        self.pass_counts: list[int] = []
+        self.base_captures = 0
+
+    # -- phases ----------------------------------------------------------------------
+    def init(self) -> int:
+        caps = ctypes.c_uint64()
+        _check(self.ctx.ptr, N.lib().cr_solver_init(self.ptr, ctypes.byref(caps)))
+        self.base_captures = int(caps.value)
+        self.pass_counts = []
+        return self.base_captures
+
+    def step(self) -> int:
+        f = ctypes.c_uint64()
+        _check(self.ctx.ptr, N.lib().cr_solver_pass(self.ptr, ctypes.byref(f)))
+        self.pass_counts.append(int(f.value))
+        return int(f.value)
+
+    def run(self) -> list[int]:
+        cap = 1 << 14
+        buf = np.zeros(cap, dtype=np.uint64)
+        passes = ctypes.c_int32()
+        _check(self.ctx.ptr, N.lib().cr_solver_run(self.ptr, buf.ctypes.data_as(N.c_u64p), cap,
+                                                   ctypes.byref(passes)))
+        self.pass_counts = [int(x) for x in buf[: passes.value]]
+        return self.pass_counts
+
+    def verdict(self) -> Verdict:
+        v = N.CrVerdict()
+        _check(self.ctx.ptr, N.lib().cr_solver_verdict(self.ptr, ctypes.byref(v)))
+        return _verdict(v, self.k)
+
+    # -- outputs ---------------------------------------------------------------------
+    def sizes(self) -> N.CrTableSizes:
+        s = N.CrTableSizes()
+        _check(self.ctx.ptr, N.lib().cr_solver_sizes(self.ptr, ctypes.byref(s)))
+        return s
+
+    def stats(self) -> N.CrSolveStats:
+        s = N.CrSolveStats()
+        _check(self.ctx.ptr, N.lib().cr_solver_stats(self.ptr, ctypes.byref(s)))
+        return s
+
+    def states(self, out: np.ndarray | None = None) -> np.ndarray:
+        nbytes = int(self.sizes().num_states)
+        if out is None:
+            out = np.empty(nbytes, dtype=np.uint8)
+        _check(self.ctx.ptr, N.lib().cr_solver_read_states(self.ptr, out.ctypes.data_as(N.c_u8p), out.nbytes))
+        return out
+
+    def device_states(self) -> tuple[int, int]:
+        p = ctypes.c_void_p()
+        n = ctypes.c_size_t()
+        _check(self.ctx.ptr, N.lib().cr_solver_device_states(self.ptr, ctypes.byref(p), ctypes.byref(n)))
+        return int(p.value or 0), int(n.value)
+
+    def configs(self) -> np.ndarray:
+        s = self.sizes()
+        out = np.empty(int(s.config_count) * self.k, dtype=np.uint8)
+        _check(self.ctx.ptr, N.lib().cr_solver_read_configs(self.ptr, out.ctypes.data_as(N.c_u8p), out.nbytes))
+        return out
+
+    def transitions(self) -> tuple[np.ndarray, np.ndarray]:
+        total = ctypes.c_uint64()
+        _check(self.ctx.ptr, N.lib().cr_solver_build_transitions(self.ptr, ctypes.byref(total)))
+        s = self.sizes()
+        heads = np.empty(int(s.config_count) + 1, dtype=np.uint64)
+        data = np.empty(max(int(total.value), 1), dtype=np.uint64)
+        _check(self.ctx.ptr, N.lib().cr_solver_read_transitions(
+            self.ptr, heads.ctypes.data_as(N.c_u64p), heads.size, data.ctypes.data_as(N.c_u64p), data.size))
+        return heads, data[: int(total.value)]
+
+    def write_table_file(self, path: str) -> None:
+        _check(self.ctx.ptr, N.lib().cr_solver_write_table_file(self.ptr, path.encode()))
+
+    def close(self) -> None:
+        if self.ptr:
+            N.lib().cr_solver_destroy(self.ptr)
+            self.ptr = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclass
+class Result:
+    states: np.ndarray
+    pass_counts: list
+    base_captures: int
+    verdict: Verdict
+    stats: N.CrSolveStats
+
+
+def solve(ctx: Context, graph: Graph, k: int, p: int = 1, rules: int = N.CR_RULES_V1,
+          with_states: bool = True) -> Result:
+    """Build, initialise, run to the fixed point and read the verdict (and table)."""
+    with Solver(ctx, graph, k, p, rules) as s:
+        caps = s.init()
+        counts = s.run()
+        v = s.verdict()
+        st = s.states() if with_states else None
+        return Result(st, counts, caps, v, s.stats())
+
+
+def footprint(n: int, k: int, p: int = 1, rules: int = N.CR_RULES_V1) -> int:
+    return int(N.lib().cr_solver_footprint(n, k, p, rules))
+
+
+def parse_matrix(text: bytes) -> Graph:
+    """Parse matrix text with the library's own parser (Graph::Graph semantics)."""
+    L = N.lib()
+    n = ctypes.c_int32()
+    nnz = ctypes.c_size_t()
+    rc = L.cr_graph_parse(text, len(text), ctypes.byref(n), None, None, 0, ctypes.byref(nnz))
+    if rc:
+        raise N.CrGpuError(rc, "cr_graph_parse")
+    rp = np.zeros(n.value + 1, dtype=np.uint32)
+    col = np.zeros(max(nnz.value, 1), dtype=np.uint16)
+    rc = L.cr_graph_parse(text, len(text), ctypes.byref(n), rp.ctypes.data_as(N.c_u32p),
+                          col.ctypes.data_as(N.c_u16p), col.size, ctypes.byref(nnz))
+    if rc:
+        raise N.CrGpuError(rc, "cr_graph_parse")
+    adj = np.zeros((n.value, n.value), dtype=np.uint8)
+    for v in range(n.value):
+        adj[v, col[rp[v]:rp[v + 1]]] = 1
+    return Graph(adj)

@@ -1,0 +1,155 @@
+/*
+ * crgpu.h - C ABI of the GB300 k-cop retrograde solver (libcrgpu.so).
+ *
+ * The reference has no foreign-function interface: its solver path is the six-phase C++
+ * contract of app/main.cpp:11-16,
+ *
+ *     bool loadGraphFile(const char*, int k, int p);   bool buildAuxGraph();
+ *     bool initializeCaptures();   bool mainLoop();   bool findFinalResult();   bool outputData();
+ *
+ * implemented per solver translation unit (solvers/k_cops_visibility.cpp,
+ * solvers/k_cops_visibility_v2.cpp) over lib/ (Graph, AdjacencyList, AuxGraph, CacheManager).
+ * The entry points below are what that contract needs from a GPU: each one names the
+ * reference routine it replaces.  A drop-in solver translation unit that maps the six phases
+ * onto them ships as copsandrobbers_gb300/csrc/k_cops_gpu.cpp.
+ *
+ * Conventions: every function returns CR_OK (0) or a positive CR_ERR_* code and never
+ * throws; cr_context_last_error() gives the message of the last failure on that context.
+ * No C++ or CUDA types cross the boundary.  One context per host thread.  All pointers are
+ * host pointers unless a name says "device".
+ */
+#ifndef CRGPU_H
+#define CRGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CR_OK 0
+#define CR_ERR_INVALID 1   /* bad argument or malformed graph */
+#define CR_ERR_NOMEM 2     /* device memory exhausted or footprint admission refused */
+#define CR_ERR_CUDA 3      /* a CUDA runtime call failed */
+#define CR_ERR_LIMIT 4     /* size beyond what this build supports (n, k, config count) */
+#define CR_ERR_INTERNAL 5  /* a device-side consistency check failed */
+#define CR_ERR_BUDGET 6    /* the pass budget ran out before the fixed point */
+#define CR_ERR_IO 7        /* file could not be read or written */
+#define CR_ERR_STATE 8     /* phase called out of order */
+
+/* Rule sets (the two live solvers of the reference). */
+#define CR_RULES_V1 1 /* solvers/k_cops_visibility.cpp: 2p DP columns per cycle */
+#define CR_RULES_V2 2 /* solvers/k_cops_visibility_v2.cpp: one plane, macro-turn search */
+
+#define CR_MAX_K 4      /* cops per configuration handled by the device kernels */
+#define CR_MAX_N 1024   /* vertices */
+
+typedef struct cr_context cr_context;
+typedef struct cr_solver cr_solver;
+
+/* A graph as out-neighbour lists: row v holds the columns set in row v of the reference's
+ * adjacency matrix, ascending (lib/src/AdjacencyList.cpp:33-76). */
+typedef struct cr_graph {
+    int32_t n;
+    const uint32_t* row_ptr; /* n + 1 entries */
+    const uint16_t* col_idx; /* row_ptr[n] entries */
+} cr_graph;
+
+/* findFinalResult (solvers/k_cops_visibility.cpp:301-354): the first configuration whose
+ * column-0 row is all marked, with the strictly smallest worst case. */
+typedef struct cr_verdict {
+    int32_t win;             /* 1 = WIN, 0 = LOSS */
+    int32_t capture_plies;   /* worst case of the best start; 127 on LOSS */
+    int64_t best_config;     /* lexicographic config id, -1 on LOSS */
+    uint16_t positions[CR_MAX_K];
+} cr_verdict;
+
+/* Sizes of the sections of the reference's table file (lib/include/CacheManager.h:33-46). */
+typedef struct cr_table_sizes {
+    uint64_t config_count;
+    uint64_t num_states;       /* config_count * n * columns */
+    int32_t columns;
+    int32_t k;
+    int32_t n;
+    int32_t pad;
+    uint64_t transitions;      /* entries of the successor CSR, 0 until built */
+} cr_table_sizes;
+
+/* Timing and traffic of the last solve, device-side (CUDA events on the solver's stream). */
+typedef struct cr_solve_stats {
+    double init_ms;            /* initializeCaptures */
+    double main_ms;            /* mainLoop to the fixed point */
+    double cop_step_ms;        /* sum over cop-turn kernel launches (when profiling) */
+    int64_t cop_step_launches;
+    int64_t kernel_launches;   /* kernels of this library launched by the solve */
+    int32_t passes;
+    int32_t slots;             /* value slots per frontier row that the solve used */
+    uint64_t resolved;         /* marked states at the fixed point */
+} cr_solve_stats;
+
+/* ---- context ------------------------------------------------------------------------ */
+
+/* stream: a cudaStream_t to launch on, or NULL for a stream owned by the context. */
+int cr_context_create(int32_t device, void* stream, cr_context** out);
+int cr_context_destroy(cr_context* ctx);
+const char* cr_context_last_error(const cr_context* ctx);
+/* Bytes of device memory a solve of this size holds (footprint admission). */
+uint64_t cr_solver_footprint(int32_t n, int32_t k, int32_t p, int32_t rules);
+/* 1 = time every cop-turn launch with CUDA events (fills cop_step_ms), 0 = off. */
+int cr_context_set_profiling(cr_context* ctx, int32_t on);
+
+/* ---- graph input (lib/src/Graph.cpp:15-79, lib/src/AdjacencyList.cpp:33-76) -------- */
+
+/* Parse adjacency-matrix text exactly as Graph::Graph does.  Two-call sizing: with
+ * row_ptr == NULL only *n and *nnz are written.  *n == 0 means the reference would reject
+ * the file ("Graph is empty or failed to load"). */
+int cr_graph_parse(const char* text, size_t len, int32_t* n, uint32_t* row_ptr,
+                   uint16_t* col_idx, size_t col_cap, size_t* nnz);
+
+/* ---- one solve, phase by phase --------------------------------------------------------- */
+
+/* buildAuxGraph (k_cops_visibility.cpp:59-83 / v2:170-198; AuxGraph::constructFrom,
+ * AuxGraph.h:59-79): allocate the device state store for (graph, k, p, rules) and build the
+ * configuration table on the device. */
+int cr_solver_create(cr_context* ctx, const cr_graph* g, int32_t k, int32_t p, int32_t rules,
+                     cr_solver** out);
+int cr_solver_destroy(cr_solver* s);
+/* initializeCaptures (k_cops_visibility.cpp:85-127 / v2:200-224). */
+int cr_solver_init(cr_solver* s, uint64_t* base_captures);
+/* One pass of mainLoop (k_cops_visibility.cpp:142-296 / v2:437-562): *new_wins receives the
+ * "Pass i: Found x new winning states" count.  0 means the fixed point was reached. */
+int cr_solver_pass(cr_solver* s, uint64_t* new_wins);
+/* mainLoop to the fixed point: pass_counts[i] for i < *passes (the final 0 included). */
+int cr_solver_run(cr_solver* s, uint64_t* pass_counts, int32_t cap, int32_t* passes);
+/* findFinalResult (k_cops_visibility.cpp:301-354 / v2:567-619). */
+int cr_solver_verdict(cr_solver* s, cr_verdict* out);
+int cr_solver_sizes(cr_solver* s, cr_table_sizes* out);
+int cr_solver_stats(cr_solver* s, cr_solve_stats* out);
+/* The states section of the table file (CacheManager.h:67): byte = marked | round << 1. */
+int cr_solver_read_states(cr_solver* s, uint8_t* dst, size_t bytes);
+/* Device pointer to the same table (valid until cr_solver_destroy). */
+int cr_solver_device_states(cr_solver* s, void** dev_ptr, size_t* bytes);
+/* The configs section (CacheManager.h:64): config_count * k bytes; n must be <= 256. */
+int cr_solver_read_configs(cr_solver* s, uint8_t* dst, size_t bytes);
+/* AuxGraph::createTransitions (AuxGraph.h:179-275) on the device: per-config successor
+ * list, sorted and deduplicated, entries = next config id * n.  Fills sizes.transitions. */
+int cr_solver_build_transitions(cr_solver* s, uint64_t* total);
+int cr_solver_read_transitions(cr_solver* s, uint64_t* heads, size_t heads_len,
+                               uint64_t* data, size_t data_len);
+/* outputData (k_cops_visibility.cpp:356-373; CacheManager::saveAuxGraph, CacheManager.h:28-75):
+ * write the whole table file (96-byte header, configs, heads, transitions, states). */
+int cr_solver_write_table_file(cr_solver* s, const char* path);
+
+/* ---- whole solves ---------------------------------------------------------------------- */
+
+/* loadGraphFile..findFinalResult in one call.  states_out (host, may be NULL) receives the
+ * states section; pass_counts (may be NULL) the per-pass counts. */
+int cr_solve(cr_context* ctx, const cr_graph* g, int32_t k, int32_t p, int32_t rules,
+             uint8_t* states_out, size_t states_bytes, uint64_t* pass_counts, int32_t cap,
+             int32_t* passes, cr_verdict* verdict, cr_solve_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CRGPU_H */

@@ -1,0 +1,343 @@
+#!/usr/bin/env python3
+"""Benchmark of the k-cop retrograde solve on one GB300 (replicas when --gpus N > 1).
+
+Workload (default "large"): the seeded connected 4-regular graph on n=256 vertices
+(configuration model, seed 12345), k=3 cops, full visibility (p=1), v1 rules -- the large
+single solve.  S = C(258,3) * 256 * 2 = 1,448,476,672 states.
+
+A step is one whole solve with the graph resident in HBM: initializeCaptures plus mainLoop
+to the fixed point (every pass, with its host read of the pass count).  The state store
+(2.0 GB) is larger than L2, so no flush is needed between steps.
+
+  value   resolved states/s = S * steps / device time, CUDA events on the solver's stream
+  e2e     the same metric through the public C ABI call cr_solve() from host CSR arrays in
+          pinned memory to the states table back in pinned host memory, every step
+  roofline  the cop-turn kernel (the dominant one): algorithmic bytes per launch / mean
+          launch time (CUDA events around each launch in a separate profiled solve)
+  cpu_baseline  the oracle's C restatement of the reference sweep on all host cores, timed on
+          a bounded sample (one pass over a slice of the configurations), scaled to a solve
+
+--impl reference times that same CPU restatement as the reference arm (the reference itself
+cannot be built on the GPU host: its sources are not there).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+LARGE = {"workload": "large single solve: seeded connected 4-regular graph, n=256 (configuration "
+                     "model, seed 12345), k=3 cops, p=1, v1 rules",
+         "n": 256, "k": 3, "p": 1, "rules": "v1", "graph_seed": 12345,
+         "l2": "state store 2.0 GB > L2 (129 MB): no flush needed"}
+METRIC = "resolved states/s"
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() in ("active", "1"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm() -> tuple[float, str]:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def traffic_per_launch() -> float | None:
+    """DRAM bytes per cop-turn launch from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "k_cop_large_n256.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_baseline(graph, k: int, p: int, passes: int, budget_s: float = 20.0) -> dict:
+    """The oracle's restatement of the reference sweep on all host cores over a bounded sample."""
+    from oracle import oracle as O
+
+    samp = O.SweepSample(graph, k, p)
+    cores = os.cpu_count() or 1
+    C = samp.count
+    slice_cfg = max(1, C // 64)
+    done_cfg, t_total, c0 = 0, 0.0, 0
+    while t_total < budget_s and c0 < C:
+        c1 = min(C, c0 + slice_cfg)
+        t = time.perf_counter()
+        samp.run(c0, c1, cores)
+        t_total += time.perf_counter() - t
+        done_cfg += c1 - c0
+        c0 = c1
+    swept = done_cfg * graph.n * 2 * p
+    rate = swept / t_total / passes
+    return {"value": rate, "unit": METRIC, "cores": cores, "kind": "port",
+            "sample": f"one v1 pass (all {2 * p} columns) over {done_cfg} of {C} configurations "
+                      f"({swept} states, {t_total:.1f} s), scaled by the solve's {passes} passes"}
+
+
+def run_reference(args) -> None:
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    from copsandrobbers_gb300 import graphs as G
+    from oracle import oracle as O
+
+    g = G.regular4(LARGE["n"], LARGE["graph_seed"])
+    k, p = LARGE["k"], LARGE["p"]
+    samp = O.SweepSample(g, k, p)
+    cores = os.cpu_count() or 1
+    C = samp.count
+    slice_cfg = max(1, C // 64)
+    passes = 5  # the pass count of this solve (the GPU arm and the oracle both find 5)
+
+    def step(i):
+        c0 = (i * slice_cfg) % C
+        c1 = min(C, c0 + slice_cfg)
+        t = time.perf_counter()
+        samp.run(c0, c1, cores)
+        return time.perf_counter() - t, (c1 - c0) * g.n * 2 * p
+
+    for i in range(args.warmup):
+        step(i)
+    t_sum, s_sum = 0.0, 0
+    for i in range(args.steps):
+        dt, st = step(args.warmup + i)
+        t_sum += dt
+        s_sum += st
+    value = s_sum / t_sum / passes
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "states/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_sum / max(args.steps, 1), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded generator)", "config": LARGE,
+        "cpu_baseline": {"value": value, "unit": "states/s", "cores": cores, "kind": "port",
+                         "sample": f"per step one v1 pass over {slice_cfg} of {C} configurations, "
+                                   f"scaled by the solve's {passes} passes"},
+        "e2e": {"value": value, "unit": "states/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args) -> None:
+    import torch
+
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    from copsandrobbers_gb300 import graphs as G
+    from copsandrobbers_gb300 import native as N
+    from copsandrobbers_gb300.solver import Context, Solver
+
+    g = G.regular4(LARGE["n"], LARGE["graph_seed"])
+    k, p = LARGE["k"], LARGE["p"]
+    stream = torch.cuda.Stream()
+    ctx = Context(local, stream.cuda_stream)
+    solver = Solver(ctx, g, k, p, N.CR_RULES_V1)
+    sizes = solver.sizes()
+    S = int(sizes.num_states)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # warm-up solves
+    for _ in range(args.warmup):
+        solver.init()
+        solver.run()
+    launches_per_step = int(solver.stats().kernel_launches)
+    passes = len(solver.pass_counts)
+
+    # timed region: K whole solves on the solver's stream
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    barrier()
+    with ClockSampler(local) as clocks:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            solver.init()
+            solver.run()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = S * args.steps * world / (ms / 1e3)
+    verdict = solver.verdict()
+
+    # roofline: time each cop-turn launch in one profiled solve
+    ctx.set_profiling(True)
+    solver.init()
+    solver.run()
+    st = solver.stats()
+    ctx.set_profiling(False)
+    cop_launches = int(st.cop_step_launches)
+    mean_ms = st.cop_step_ms / max(cop_launches, 1)
+    C, n = int(sizes.config_count), int(sizes.n)
+    rwp = ((n + 31) // 32 + 3) // 4 * 4 if (n + 31) // 32 > 2 else (n + 31) // 32
+    slots = int(st.slots)
+    # algorithmic bytes of one cop-turn launch: read every config's marked row and its input
+    # frontier row (all value slots) once, read+write the frontier flags, write the new marks
+    cop_marks = sum(solver.pass_counts) / 2.0 / max(cop_launches, 1)
+    alg_bytes = C * (4 * rwp * (1 + slots) + 2) + cop_marks * (1 + 4.0 / 32)
+    achieved = alg_bytes / (mean_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peak_hbm()
+    traffic = traffic_per_launch()
+    solver.close()
+
+    # e2e: the public one-call API from pinned host CSR to the pinned host table
+    import ctypes
+    import numpy as np
+    row_ptr, col = g.csr()
+    rp_pin = torch.from_numpy(row_ptr.view(np.int32)).pin_memory()
+    col_pin = torch.from_numpy(col.view(np.int16)).pin_memory()
+    out_pin = torch.empty(S, dtype=torch.uint8, pin_memory=True)
+    cg = N.CrGraph(n, ctypes.cast(rp_pin.data_ptr(), N.c_u32p), ctypes.cast(col_pin.data_ptr(), N.c_u16p))
+    counts = np.zeros(1024, dtype=np.uint64)
+    npass = ctypes.c_int32()
+    vv = N.CrVerdict()
+    L = N.lib()
+
+    def e2e_step():
+        rc = L.cr_solve(ctx.ptr, ctypes.byref(cg), k, p, N.CR_RULES_V1,
+                        ctypes.cast(out_pin.data_ptr(), N.c_u8p), S, counts.ctypes.data_as(N.c_u64p),
+                        1024, ctypes.byref(npass), ctypes.byref(vv), None)
+        if rc:
+            raise RuntimeError(f"cr_solve failed: {rc} {L.cr_context_last_error(ctx.ptr)}")
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    torch.cuda.synchronize()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    e2e_ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([e2e_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = S * args.steps * world / (e2e_ms / 1e3)
+
+    line = None
+    if rank == 0:
+        base = cpu_baseline(g, k, p, passes) if not args.no_cpu_baseline else None
+        line = {
+            "metric": METRIC, "value": value, "unit": "states/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+            "data": "synthetic (seeded generator, committed as tests/golden/graphs/regular4_n256_s12345.txt)",
+            "config": dict(LARGE, parallelism=f"replicas x{world}" if world > 1 else "single GPU",
+                           passes=passes, verdict="WIN" if verdict.win else "LOSS"),
+            "e2e": {"value": e2e_value, "unit": "states/s",
+                    "h2d_bytes_per_step": int(row_ptr.nbytes + col.nbytes),
+                    "d2h_bytes_per_step": int(S + 8 * len(counts) + ctypes.sizeof(vv))},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "kernel": "k_cop (cop turn)",
+                         "peak_source": peak_kind, "launches": cop_launches, "mean_launch_ms": mean_ms,
+                         "alg_bytes_per_launch": alg_bytes},
+            "cpu_baseline": base,
+            "clocks": clocks.summary(),
+            "gpu_launches": launches_per_step * args.steps,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,85 @@
+"""Command line: solve one graph on the GPU, or write a seeded synthetic graph.
+
+  python -m copsandrobbers_gb300.cli solve GRAPH.txt -k 3 -p 1 [--rules v1|v2] [--repeat R]
+  python -m copsandrobbers_gb300.cli solve --gen regular4:256:12345 -k 3
+  python -m copsandrobbers_gb300.cli gen regular4:256:12345 out.txt
+
+Generator specs: regular4:N:SEED, er:N:MEAN_DEGREE:SEED, delaunay:N:SEED[:MEAN_DEGREE].
+"""
+from __future__ import annotations
+
+import argparse
+import hashlib
+import sys
+import time
+
+from . import graphs as G
+from . import native as N
+
+
+def graph_from_spec(spec: str) -> G.Graph:
+    kind, *a = spec.split(":")
+    if kind == "regular4":
+        return G.regular4(int(a[0]), int(a[1]))
+    if kind == "er":
+        return G.erdos_renyi(int(a[0]), float(a[1]), int(a[2]))
+    if kind == "delaunay":
+        return G.delaunay_thinned(int(a[0]), int(a[1]), float(a[2]) if len(a) > 2 else 4.5)
+    raise SystemExit(f"unknown generator spec {spec!r}")
+
+
+def cmd_solve(args) -> int:
+    from .solver import Context, Solver
+
+    g = graph_from_spec(args.gen) if args.gen else G.load_matrix(args.graph)
+    rules = N.CR_RULES_V2 if args.rules == "v2" else N.CR_RULES_V1
+    with Context(args.device) as ctx:
+        ctx.set_profiling(args.profile)
+        with Solver(ctx, g, args.k, args.p, rules) as s:
+            for _ in range(args.repeat):
+                t0 = time.perf_counter()
+                caps = s.init()
+                counts = s.run()
+                dt = time.perf_counter() - t0
+            v = s.verdict()
+            st = s.stats()
+            print(f"n={g.n} k={args.k} p={args.p} rules={args.rules}: base captures {caps}, passes {counts}")
+            print(f"verdict: {'WIN' if v.win else 'LOSS'} start {v.positions} capture {v.capture_plies} plies")
+            print(f"init {st.init_ms:.3f} ms, main loop {st.main_ms:.3f} ms, wall {dt * 1e3:.3f} ms, "
+                  f"states {s.sizes().num_states}, kernel launches {st.kernel_launches}")
+            if args.digest:
+                print("states sha256", hashlib.sha256(s.states().tobytes()).hexdigest())
+    return 0
+
+
+def cmd_gen(args) -> int:
+    G.save_matrix(graph_from_spec(args.spec), args.out)
+    return 0
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser(prog="copsandrobbers_gb300.cli", description=__doc__.split("\n")[0])
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    s = sub.add_parser("solve")
+    s.add_argument("graph", nargs="?")
+    s.add_argument("--gen")
+    s.add_argument("-k", type=int, required=True)
+    s.add_argument("-p", type=int, default=1)
+    s.add_argument("--rules", choices=["v1", "v2"], default="v1")
+    s.add_argument("--device", type=int, default=0)
+    s.add_argument("--repeat", type=int, default=1)
+    s.add_argument("--profile", action="store_true")
+    s.add_argument("--digest", action="store_true")
+    s.set_defaults(fn=cmd_solve)
+    g = sub.add_parser("gen")
+    g.add_argument("spec")
+    g.add_argument("out")
+    g.set_defaults(fn=cmd_gen)
+    args = ap.parse_args(argv)
+    if args.cmd == "solve" and not (args.graph or args.gen):
+        ap.error("solve needs GRAPH.txt or --gen SPEC")
+    return args.fn(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -23,6 +23,8 @@ void launch_verdict(const V1Dev& d, int cols, unsigned long long* best, int grid
 void launch_popcount(const uint32_t* plane, size_t words, unsigned long long* out, int grid,
                      cudaStream_t st);
 int max_cop_blocks_per_sm(int k, int rwp, int S);
+bool pull_supported(int S, int rwp);
+int cop_launches(int direct);
 size_t cop_smem_bytes(int S, int rwp);
 size_t and_smem_bytes(int S, int rwp, int n);
 void launch_unrank(const uint32_t* B, int n, int k, uint32_t C, uint16_t* out, int grid, cudaStream_t st);
@@ -64,6 +66,12 @@ struct cr_solver {
     uint32_t* d_marked = nullptr;
     uint32_t* d_front = nullptr;
     uint8_t* d_fflag = nullptr;
+    uint32_t* d_cand = nullptr;
+    uint8_t* d_cflag = nullptr;
+    uint32_t* d_rrp = nullptr;
+    uint16_t* d_rcol = nullptr;
+    uint32_t* d_nbr = nullptr;
+    uint32_t* d_iso = nullptr;
     ColMeta* d_meta = nullptr;
     unsigned long long* d_counters = nullptr;  // [0] pass_new, [1] verdict key, [2] scratch
     unsigned int* d_err = nullptr;
@@ -211,6 +219,7 @@ uint64_t cr_solver_footprint(int32_t n, int32_t k, int32_t p, int32_t rules) {
     uint64_t b = C * (uint64_t)n * cols;                 // table
     b += (uint64_t)cols * C * rwp * 4;                   // marked
     b += (uint64_t)cols * C * S * rwp * 4;               // frontiers
+    b += C * S * rwp * 4 + C;                            // push-mode candidate rows and flags
     b += (uint64_t)cols * C;                             // flags
     b += C * (uint64_t)k * 2;                            // configs
     b += (uint64_t)n * rwp * 4 + (uint64_t)k * (n + 1) * 4 + (1u << 16);
@@ -222,13 +231,14 @@ static void free_v1(cr_solver* s) {
     s->pass_graph = nullptr;
     void* ptrs[] = {s->d_rp, s->d_col, s->d_binom, s->d_configs, s->d_hop, s->d_table,
                     s->d_marked, s->d_front, s->d_fflag, s->d_meta, s->d_counters, s->d_err,
-                    s->d_heads, s->d_trans};
+                    s->d_heads, s->d_trans, s->d_cand, s->d_cflag, s->d_rrp, s->d_rcol, s->d_nbr, s->d_iso};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     s->d_rp = nullptr; s->d_col = nullptr; s->d_binom = nullptr; s->d_configs = nullptr;
     s->d_hop = nullptr; s->d_table = nullptr; s->d_marked = nullptr; s->d_front = nullptr;
     s->d_fflag = nullptr; s->d_meta = nullptr; s->d_counters = nullptr; s->d_err = nullptr;
-    s->d_heads = nullptr; s->d_trans = nullptr;
+    s->d_heads = nullptr; s->d_trans = nullptr; s->d_cand = nullptr; s->d_cflag = nullptr;
+    s->d_rrp = nullptr; s->d_rcol = nullptr; s->d_nbr = nullptr; s->d_iso = nullptr;
     if (s->h_pinned) cudaFreeHost(s->h_pinned);
     s->h_pinned = nullptr;
     cudaEvent_t evs[] = {s->ev0, s->ev1, s->evc0, s->evc1};
@@ -244,6 +254,11 @@ static V1Dev dev_view(const cr_solver* s) {
     d.g.rwp = s->rwp;
     d.g.row_ptr = s->d_rp;
     d.g.col = s->d_col;
+    d.g.rrow_ptr = s->d_rrp;
+    d.g.rcol = s->d_rcol;
+    d.g.nbr = s->d_nbr;
+    d.g.isolated = s->d_iso;
+    d.g.maxdeg = s->maxdeg;
     d.k = s->k;
     d.cols = s->cols;
     d.S = s->S;
@@ -255,6 +270,8 @@ static V1Dev dev_view(const cr_solver* s) {
     d.marked = s->d_marked;
     d.front = s->d_front;
     d.fflag = s->d_fflag;
+    d.cand = s->d_cand;
+    d.cflag = s->d_cflag;
     d.meta = s->d_meta;
     d.pass_new = s->d_counters;
     d.err = s->d_err;
@@ -289,9 +306,37 @@ static int alloc_v1(cr_solver* s) {
     CR_CUDA(ctx, cudaMalloc(&s->d_front, (size_t)s->cols * C * s->S * s->rwp * 4));
     CR_CUDA(ctx, cudaMalloc(&s->d_fflag, (size_t)s->cols * C));
     CR_CUDA(ctx, cudaMalloc(&s->d_meta, sizeof(ColMeta) * s->cols));
+    CR_CUDA(ctx, cudaMalloc(&s->d_cand, C * s->S * s->rwp * 4));
+    CR_CUDA(ctx, cudaMalloc(&s->d_cflag, C));
+    CR_CUDA(ctx, cudaMemsetAsync(s->d_cand, 0, C * s->S * s->rwp * 4, ctx->stream));
+    CR_CUDA(ctx, cudaMemsetAsync(s->d_cflag, 0, C, ctx->stream));
     CR_CUDA(ctx, cudaMalloc(&s->d_hop, (size_t)s->n * s->rwp * 4));
     std::vector<uint32_t> hop = hop_masks(s);
     CR_CUDA(ctx, cudaMemcpyAsync(s->d_hop, hop.data(), hop.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+    // out-neighbour masks (capture-seed closed form) and the in-neighbour CSR (push mode)
+    std::vector<uint32_t> nbr((size_t)s->n * s->rwp, 0);
+    std::vector<uint32_t> rrp(s->n + 1, 0);
+    for (uint32_t e = 0; e < s->h_col.size(); ++e) rrp[s->h_col[e] + 1]++;
+    for (int v = 0; v < s->n; ++v) rrp[v + 1] += rrp[v];
+    std::vector<uint16_t> rcol(std::max<size_t>(s->h_col.size(), 1));
+    std::vector<uint32_t> fill(rrp.begin(), rrp.end() - 1);
+    for (int u = 0; u < s->n; ++u)
+        for (uint32_t e = s->h_rp[u]; e < s->h_rp[u + 1]; ++e) {
+            const int v = s->h_col[e];
+            nbr[(size_t)u * s->rwp + (v >> 5)] |= 1u << (v & 31);
+            rcol[fill[v]++] = (uint16_t)u;  // in-neighbours of v, ascending u
+        }
+    std::vector<uint32_t> iso(s->rwp, 0);
+    for (int v = 0; v < s->n; ++v)
+        if (s->h_rp[v + 1] == s->h_rp[v]) iso[v >> 5] |= 1u << (v & 31);
+    CR_CUDA(ctx, cudaMalloc(&s->d_iso, iso.size() * 4));
+    CR_CUDA(ctx, cudaMemcpyAsync(s->d_iso, iso.data(), iso.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CR_CUDA(ctx, cudaMalloc(&s->d_nbr, nbr.size() * 4));
+    CR_CUDA(ctx, cudaMalloc(&s->d_rrp, rrp.size() * 4));
+    CR_CUDA(ctx, cudaMalloc(&s->d_rcol, rcol.size() * 2));
+    CR_CUDA(ctx, cudaMemcpyAsync(s->d_nbr, nbr.data(), nbr.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CR_CUDA(ctx, cudaMemcpyAsync(s->d_rrp, rrp.data(), rrp.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CR_CUDA(ctx, cudaMemcpyAsync(s->d_rcol, rcol.data(), rcol.size() * 2, cudaMemcpyHostToDevice, ctx->stream));
     CR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return CR_OK;
 }
@@ -371,8 +416,8 @@ int cr_solver_create(cr_context* ctx, const cr_graph* g, int32_t k, int32_t p, i
         CR_TRY(cudaGetLastError());
     }
     if (rules == CR_RULES_V1) {
-        if ((uint64_t)s->S * s->rwp / std::min(s->rwp, 4) > 32)
-            return (fail(ctx, CR_ERR_LIMIT, "row too wide for the warp layout"), bail(CR_ERR_LIMIT));
+        if (!pull_supported(s->S, s->rwp))
+            return (fail(ctx, CR_ERR_LIMIT, "v1 rules: rows of %d vertices exceed the warp layout (n <= 512)", s->n), bail(CR_ERR_LIMIT));
         int rc = alloc_v1(s);
         if (rc) return bail(rc);
         const int per_sm = max_cop_blocks_per_sm(k, s->rwp, s->S);
@@ -419,14 +464,14 @@ static int v1_init(cr_solver* s, uint64_t* caps) {
     CR_CUDA(ctx, cudaEventRecord(s->ev0, st));
     CR_CUDA(ctx, cudaMemsetAsync(s->d_table, kUnmarked, C * s->n * s->cols, st));
     CR_CUDA(ctx, cudaMemsetAsync(s->d_marked, 0, (size_t)s->cols * C * s->rwp * 4, st));
-    CR_CUDA(ctx, cudaMemsetAsync(s->d_front, 0, (size_t)2 * C * s->S * s->rwp * 4, st));
     CR_CUDA(ctx, cudaMemsetAsync(s->d_fflag, 0, (size_t)s->cols * C, st));
     CR_CUDA(ctx, cudaMemsetAsync(s->d_counters, 0, 4 * sizeof(unsigned long long), st));
     CR_CUDA(ctx, cudaMemsetAsync(s->d_err, 0, sizeof(unsigned), st));
     std::vector<ColMeta> meta(s->cols);
-    for (int c = 0; c < s->cols; ++c) meta[c] = ColMeta{0, kEmptyLo, -1, 0};
-    meta[0] = ColMeta{0, 0, 0, 1};  // capture seeds; pass 1's column-0 producer appends to them
-    meta[1] = ColMeta{0, 0, 0, 0};
+    for (int c = 0; c < s->cols; ++c) meta[c] = ColMeta{0, kEmptyLo, -1, 0, 0, 0, {0, 0}};
+    // capture seeds in columns 0 and 1; pass 1's column-0 producer appends to column 0's
+    meta[0] = ColMeta{0, 0, 0, 1, (int)std::min<uint64_t>(C, INT32_MAX), 0, {0, 0}};
+    meta[1] = ColMeta{0, 0, 0, 0, (int)std::min<uint64_t>(C, INT32_MAX), 1, {0, 0}};
     CR_CUDA(ctx, cudaMemcpyAsync(s->d_meta, meta.data(), sizeof(ColMeta) * s->cols, cudaMemcpyHostToDevice, st));
     V1Dev d = dev_view(s);
     launch_init(d, s->grid_small, st);
@@ -494,7 +539,10 @@ static int v1_pass(cr_solver* s, uint64_t* found) {
         CR_CUDA(ctx, cudaGraphLaunch(s->pass_graph, st));
     }
     CR_CUDA(ctx, cudaStreamSynchronize(st));
-    s->stats.kernel_launches += 2 * s->cols;
+    int per_pass = s->cols;  // prep kernels
+    for (int col = 0; col < s->cols; ++col)
+        per_pass += col % 2 == 0 ? cop_launches(0) : (col < s->cols - 1 ? cop_launches(1) : 1);
+    s->stats.kernel_launches += per_pass;
     *found = s->h_pinned[0];
     return CR_OK;
 }
@@ -525,12 +573,17 @@ static int grow_slots_and_replay(cr_solver* s) {
     std::vector<uint64_t> done = s->pass_counts;
     cudaFree(s->d_front);
     s->d_front = nullptr;
+    cudaFree(s->d_cand);
+    s->d_cand = nullptr;
     if (s->pass_graph) cudaGraphExecDestroy(s->pass_graph);
     s->pass_graph = nullptr;
     s->S *= 2;
-    if ((uint64_t)s->S * s->rwp / std::min(s->rwp, 4) > 32)
+    if (!pull_supported(s->S, s->rwp))
         return fail(ctx, CR_ERR_LIMIT, "row too wide for %d value slots", s->S);
     CR_CUDA(ctx, cudaMalloc(&s->d_front, (size_t)s->cols * s->C * s->S * s->rwp * 4));
+    CR_CUDA(ctx, cudaMalloc(&s->d_cand, (size_t)s->C * s->S * s->rwp * 4));
+    CR_CUDA(ctx, cudaMemsetAsync(s->d_cand, 0, (size_t)s->C * s->S * s->rwp * 4, ctx->stream));
+    CR_CUDA(ctx, cudaMemsetAsync(s->d_cflag, 0, s->C, ctx->stream));
     const int per_sm = max_cop_blocks_per_sm(s->k, s->rwp, s->S);
     s->grid_cop = (int)std::max<uint64_t>(1, std::min<uint64_t>((s->C + 7) / 8, (uint64_t)ctx->num_sms * per_sm));
     uint64_t caps;

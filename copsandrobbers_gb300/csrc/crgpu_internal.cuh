@@ -26,20 +26,32 @@ constexpr unsigned kErrSlot = 1u;    // a value fell outside the frontier's valu
 constexpr unsigned kErrRank = 2u;    // a successor rank fell outside [0, C)
 constexpr unsigned kErrBudget = 4u;  // a bounded device loop ran out
 
+// A frontier with fewer non-empty rows than C / kPushRatio is pushed to its predecessors
+// (scatter with atomic ORs); a denser one is pulled by every configuration (gather).
+constexpr int kPushRatio = 16;
+
 // Range and base of the value slots of one column's frontier.
 struct ColMeta {
     int base;    // value of slot 0
     int lo;      // smallest value in the frontier (kEmptyLo when empty)
     int hi;      // largest value in the frontier (-1 when empty)
     int append;  // 1 = the next producer run adds to the frontier instead of replacing it
+    int rows;    // configurations whose frontier row is non-empty
+    int seed;    // 1 = the frontier is exactly the capture seeds (r on a cop, value 0)
+    int pad[2];
 };
 
 struct DevGraph {
     int n;
+    int maxdeg;           // largest out-degree
     int rw;               // 32-bit words per robber row
     int rwp;              // padded words per row
     const uint32_t* row_ptr;  // n + 1
     const uint16_t* col;      // out-neighbours, ascending
+    const uint32_t* rrow_ptr; // n + 1: in-neighbours (predecessor moves)
+    const uint16_t* rcol;
+    const uint32_t* nbr;      // [n][rwp]: out-neighbour masks
+    const uint32_t* isolated; // [rwp]: vertices without out-neighbours
 };
 
 // Everything one v1 solve's kernels touch.
@@ -54,6 +66,8 @@ struct V1Dev {
     uint32_t* marked;
     uint32_t* front;
     uint8_t* fflag;
+    uint32_t* cand;           // [C][S][rwp]: push-mode OR of successor frontier rows
+    uint8_t* cflag;           // [C]: 1 = cand row non-empty
     ColMeta* meta;            // [cols]
     unsigned long long* pass_new;
     unsigned int* err;

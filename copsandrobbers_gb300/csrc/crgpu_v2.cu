@@ -178,6 +178,7 @@ __device__ __forceinline__ uint32_t move_target(const Moves<K>& mv, int t, const
 // Phase D boundary (v2:321-334): cloud within the marked set of config cid -> 2p + max round.
 template <int W>
 __device__ __forceinline__ int leaf_cost(const V2Dev& d, uint32_t cid, const Mask<W>& V) {
+    if (cid >= d.C) return kV2None;  // never taken for a well-formed rank table
     const uint32_t* mrow = d.marked + (size_t)cid * d.rwp;
 #pragma unroll
     for (int j = 0; j < W; ++j)
@@ -329,7 +330,7 @@ __global__ void __launch_bounds__(256) k_v2_root(V2Dev d) {
                 Mask<W> v1 = nr;
                 mask_clear<W, K>(v1, c1);
                 if (mask_empty<W>(v1)) { best = min(best, 2); continue; }
-                best = min(best, (int)d.val1[(size_t)cid1 * d.n + r]);
+                if (cid1 < d.C) best = min(best, (int)d.val1[(size_t)cid1 * d.n + r]);
             }
             if (live) {
                 const int v = best < kMaxRound ? best : kV2None;
@@ -392,7 +393,8 @@ __global__ void k_v2_dilate(const uint8_t* __restrict__ in, uint8_t* out, const 
         uint8_t any = 0;
         for (int t = 0; t < mv.T && !any; ++t) {
             int cc[K];
-            any = in[move_target<K>(mv, t, adj, B, np1, cc)];
+            const uint32_t s = move_target<K>(mv, t, adj, B, np1, cc);
+            any = s < C ? in[s] : 0;
         }
         out[c] = any ? 1 : 0;
     }

@@ -143,21 +143,40 @@ static size_t max_fanout(const or_graph* g, int k, int cop_stay) {
 }
 
 /* Transition CSR: heads[count + 1] and, when data != NULL, data[heads[count]].
- * Call once with data == NULL to size it. */
+ * Call once with data == NULL to size it.  Configs are independent, so both calls split them
+ * across threads; the result is identical to the serial build. */
 int or_transitions(int n, const uint32_t* row_ptr, const uint16_t* col, int k, int cop_stay,
                    const uint16_t* configs, uint64_t count, uint64_t* heads, uint64_t* data) {
     or_graph g = {n, row_ptr, col};
     size_t cap = max_fanout(&g, k, cop_stay);
-    heads[0] = 0;
-    uint64_t* buf = (uint64_t*)malloc(cap * sizeof(uint64_t));
-    if (!buf) return 1;
-    for (uint64_t c = 0; c < count; ++c) {
-        size_t m = successors(&g, configs, count, k, c, cop_stay, buf);
-        if (data) memcpy(data + heads[c], buf, m * sizeof(uint64_t));
-        heads[c + 1] = heads[c] + m;
+    int fail = 0;
+    if (!data) {
+        heads[0] = 0;
+        #pragma omp parallel reduction(| : fail)
+        {
+            uint64_t* buf = (uint64_t*)malloc(cap * sizeof(uint64_t));
+            if (!buf) fail = 1;
+            #pragma omp for schedule(dynamic, 256)
+            for (int64_t c = 0; c < (int64_t)count; ++c)
+                heads[c + 1] = buf ? successors(&g, configs, count, k, (uint64_t)c, cop_stay, buf) : 0;
+            free(buf);
+        }
+        for (uint64_t c = 0; c < count; ++c) heads[c + 1] += heads[c];
+        return fail;
     }
-    free(buf);
-    return 0;
+    #pragma omp parallel reduction(| : fail)
+    {
+        uint64_t* buf = (uint64_t*)malloc(cap * sizeof(uint64_t));
+        if (!buf) fail = 1;
+        #pragma omp for schedule(dynamic, 256)
+        for (int64_t c = 0; c < (int64_t)count; ++c) {
+            if (!buf) continue;
+            size_t m = successors(&g, configs, count, k, (uint64_t)c, cop_stay, buf);
+            memcpy(data + heads[c], buf, m * sizeof(uint64_t));
+        }
+        free(buf);
+    }
+    return fail;
 }
 
 /* Exact-p-hop reachability from r (k_cops_visibility.cpp:245-262), as a byte mask. */
@@ -177,6 +196,93 @@ static void hop_set(const or_graph* g, int r, int depth, int robber_stay, uint8_
 
 /* ------------------------------------------------------------------------- v1 --- */
 
+/* One column of the v1 sweep over configs [c0, c1) (k_cops_visibility.cpp:146-290).
+ * Returns the number of states marked. */
+static uint64_t v1_column(const or_graph* g, int cols, int cl, const uint64_t* heads,
+                          const uint64_t* trans, const uint8_t* hops, uint8_t* states,
+                          int64_t c0, int64_t c1) {
+    const int n = g->n;
+    const int nx = (cl + 1) % cols;
+    uint64_t fc = 0;
+    if (cl % 2 == 0) {
+        /* cop turn: OR over transitions, min + 1 (k_cops_visibility.cpp:160-197) */
+        #pragma omp parallel for schedule(dynamic, 64) reduction(+ : fc)
+        for (int64_t c = c0; c < c1; ++c) {
+            for (int r = 0; r < n; ++r) {
+                uint8_t* s = states + ((size_t)c * n + r) * cols + cl;
+                if (*s & 1) continue;
+                int mn = OR_MAX_ROUND, win = 0;
+                for (uint64_t i = heads[c]; i < heads[c + 1]; ++i) {
+                    uint8_t v = states[(trans[i] + (uint64_t)r) * cols + nx];
+                    if (v & 1) { win = 1; if ((v >> 1) < mn) mn = v >> 1; }
+                }
+                if (win && mn + 1 < OR_MAX_ROUND) { *s = (uint8_t)(1 | ((mn + 1) << 1)); fc++; }
+            }
+        }
+    } else if (cl < cols - 1) {
+        /* deferred robber turn: direct copy + 1 (k_cops_visibility.cpp:209-228) */
+        #pragma omp parallel for schedule(dynamic, 64) reduction(+ : fc)
+        for (int64_t c = c0; c < c1; ++c) {
+            for (int r = 0; r < n; ++r) {
+                uint8_t* s = states + ((size_t)c * n + r) * cols + cl;
+                if (*s & 1) continue;
+                uint8_t v = states[((size_t)c * n + r) * cols + nx];
+                if ((v & 1) && (v >> 1) + 1 < OR_MAX_ROUND) { *s = (uint8_t)(1 | (((v >> 1) + 1) << 1)); fc++; }
+            }
+        }
+    } else {
+        /* max col: AND over the exact-p-hop cloud, max + 1 (k_cops_visibility.cpp:235-288) */
+        #pragma omp parallel for schedule(dynamic, 64) reduction(+ : fc)
+        for (int64_t c = c0; c < c1; ++c) {
+            for (int r = 0; r < n; ++r) {
+                uint8_t* s = states + ((size_t)c * n + r) * cols + cl;
+                if (*s & 1) continue;
+                const uint8_t* hv = hops + (size_t)r * n;
+                int all = 1, mx = 0;
+                for (int v = 0; v < n; ++v) {
+                    if (!hv[v]) continue;
+                    uint8_t x = states[((size_t)c * n + v) * cols + nx];
+                    if (!(x & 1)) { all = 0; break; }
+                    if ((x >> 1) > mx) mx = x >> 1;
+                }
+                if (all && mx + 1 < OR_MAX_ROUND) { *s = (uint8_t)(1 | ((mx + 1) << 1)); fc++; }
+            }
+        }
+    }
+    return fc;
+}
+
+static uint8_t* v1_hops(const or_graph* g, int p, int robber_stay) {
+    const int n = g->n;
+    uint8_t* hops = (uint8_t*)malloc((size_t)n * n);
+    uint8_t* t0 = (uint8_t*)malloc((size_t)n);
+    uint8_t* t1 = (uint8_t*)malloc((size_t)n);
+    if (!hops || !t0 || !t1) { free(hops); free(t0); free(t1); return NULL; }
+    for (int r = 0; r < n; ++r) {
+        hop_set(g, r, p, robber_stay, t0, t1);
+        memcpy(hops + (size_t)r * n, t0, (size_t)n);
+    }
+    free(t0); free(t1);
+    return hops;
+}
+
+/* initializeCaptures (k_cops_visibility.cpp:85-127). */
+uint64_t or_v1_init(int n, int k, int p, const uint16_t* configs, uint64_t count, uint8_t* states) {
+    const int cols = 2 * p;
+    uint64_t caps = 0;
+    for (uint64_t c = 0; c < count; ++c) {
+        const uint16_t* cops = configs + c * k;
+        for (int r = 0; r < n; ++r) {
+            uint8_t* s = states + ((size_t)c * n + r) * cols;
+            memset(s, OR_UNMARKED, (size_t)cols);
+            int catch_ = 0;
+            for (int i = 0; i < k; ++i) if (cops[i] == r) catch_ = 1;
+            if (catch_) { s[0] = 1; s[1] = 1; caps++; }
+        }
+    }
+    return caps;
+}
+
 /*
  * v1 solve.  states[(cid * n + r) * cols + col], cols = 2p.  pass_counts receives the
  * "Pass i: Found x new winning states" numbers (the final zero included); returns the pass
@@ -190,95 +296,46 @@ int or_v1_solve(int n, const uint32_t* row_ptr, const uint16_t* col, int k, int 
                 uint64_t* base_captures, uint64_t* pass_counts, int max_passes, int threads) {
     or_graph g = {n, row_ptr, col};
     const int cols = 2 * p;
-    (void)threads;
     (void)cop_stay; /* carried by the transition CSR passed in */
 #ifdef _OPENMP
     if (threads > 0) omp_set_num_threads(threads);
+#else
+    (void)threads;
 #endif
-    /* initializeCaptures (k_cops_visibility.cpp:85-127) */
-    uint64_t caps = 0;
-    for (uint64_t c = 0; c < count; ++c) {
-        const uint16_t* cops = configs + c * k;
-        for (int r = 0; r < n; ++r) {
-            uint8_t* s = states + ((size_t)c * n + r) * cols;
-            memset(s, OR_UNMARKED, (size_t)cols);
-            int catch_ = 0;
-            for (int i = 0; i < k; ++i) if (cops[i] == r) catch_ = 1;
-            if (catch_) { s[0] = 1; s[1] = 1; caps++; }
-        }
-    }
-    *base_captures = caps;
-
-    /* exact-p-hop sets, one per anchor */
-    uint8_t* hops = (uint8_t*)malloc((size_t)n * n);
-    uint8_t* t0 = (uint8_t*)malloc((size_t)n);
-    uint8_t* t1 = (uint8_t*)malloc((size_t)n);
-    if (!hops || !t0 || !t1) { free(hops); free(t0); free(t1); return -1; }
-    for (int r = 0; r < n; ++r) {
-        hop_set(&g, r, p, robber_stay, t0, t1);
-        memcpy(hops + (size_t)r * n, t0, (size_t)n);
-    }
-    free(t0); free(t1);
-
+    *base_captures = or_v1_init(n, k, p, configs, count, states);
+    uint8_t* hops = v1_hops(&g, p, robber_stay);
+    if (!hops) return -1;
     int passes = 0;
     for (;;) {
         if (passes >= max_passes) { free(hops); return -2; }
         uint64_t found = 0;
-        for (int cl = 0; cl < cols; ++cl) {
-            const int nx = (cl + 1) % cols;
-            uint64_t fc = 0;
-            if (cl % 2 == 0) {
-                /* cop turn: OR over transitions, min + 1 (k_cops_visibility.cpp:160-197) */
-                #pragma omp parallel for schedule(dynamic, 64) reduction(+ : fc)
-                for (int64_t c = 0; c < (int64_t)count; ++c) {
-                    for (int r = 0; r < n; ++r) {
-                        uint8_t* s = states + ((size_t)c * n + r) * cols + cl;
-                        if (*s & 1) continue;
-                        int mn = OR_MAX_ROUND, win = 0;
-                        for (uint64_t i = heads[c]; i < heads[c + 1]; ++i) {
-                            uint8_t v = states[(trans[i] + (uint64_t)r) * cols + nx];
-                            if (v & 1) { win = 1; if ((v >> 1) < mn) mn = v >> 1; }
-                        }
-                        if (win && mn + 1 < OR_MAX_ROUND) { *s = (uint8_t)(1 | ((mn + 1) << 1)); fc++; }
-                    }
-                }
-            } else if (cl < cols - 1) {
-                /* deferred robber turn: direct copy + 1 (k_cops_visibility.cpp:209-228) */
-                #pragma omp parallel for schedule(dynamic, 64) reduction(+ : fc)
-                for (int64_t c = 0; c < (int64_t)count; ++c) {
-                    for (int r = 0; r < n; ++r) {
-                        uint8_t* s = states + ((size_t)c * n + r) * cols + cl;
-                        if (*s & 1) continue;
-                        uint8_t v = states[((size_t)c * n + r) * cols + nx];
-                        if ((v & 1) && (v >> 1) + 1 < OR_MAX_ROUND) { *s = (uint8_t)(1 | (((v >> 1) + 1) << 1)); fc++; }
-                    }
-                }
-            } else {
-                /* max col: AND over the exact-p-hop cloud, max + 1 (k_cops_visibility.cpp:235-288) */
-                #pragma omp parallel for schedule(dynamic, 64) reduction(+ : fc)
-                for (int64_t c = 0; c < (int64_t)count; ++c) {
-                    for (int r = 0; r < n; ++r) {
-                        uint8_t* s = states + ((size_t)c * n + r) * cols + cl;
-                        if (*s & 1) continue;
-                        const uint8_t* hv = hops + (size_t)r * n;
-                        int all = 1, mx = 0;
-                        for (int v = 0; v < n; ++v) {
-                            if (!hv[v]) continue;
-                            uint8_t x = states[((size_t)c * n + v) * cols + nx];
-                            if (!(x & 1)) { all = 0; break; }
-                            if ((x >> 1) > mx) mx = x >> 1;
-                        }
-                        if (all && mx + 1 < OR_MAX_ROUND) { *s = (uint8_t)(1 | ((mx + 1) << 1)); fc++; }
-                    }
-                }
-            }
-            found += fc;
-        }
+        for (int cl = 0; cl < cols; ++cl)
+            found += v1_column(&g, cols, cl, heads, trans, hops, states, 0, (int64_t)count);
         pass_counts[passes++] = found;
         if (found == 0) break;
     }
     free(hops);
     return passes;
+}
+
+/* CPU-baseline sample: the columns of one v1 pass restricted to configs [c0, c1), on a table
+ * prepared by or_v1_init.  Returns the states marked. */
+uint64_t or_v1_sweep_slice(int n, const uint32_t* row_ptr, const uint16_t* col, int k, int p,
+                           const uint64_t* heads, const uint64_t* trans, uint8_t* states,
+                           int64_t c0, int64_t c1, int threads) {
+    or_graph g = {n, row_ptr, col};
+    (void)k;
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#else
+    (void)threads;
+#endif
+    uint8_t* hops = v1_hops(&g, p, 0);
+    if (!hops) return 0;
+    uint64_t found = 0;
+    for (int cl = 0; cl < 2 * p; ++cl) found += v1_column(&g, 2 * p, cl, heads, trans, hops, states, c0, c1);
+    free(hops);
+    return found;
 }
 
 /* Verdict scan over column 0 (k_cops_visibility.cpp:301-331): the first config whose every

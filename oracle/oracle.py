@@ -18,6 +18,9 @@ from dataclasses import dataclass, field
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+# Idle OpenMP workers sleep instead of spinning: the oracle often shares the host with other
+# work (a GPU process, a reference run), where spinning barriers slow every column sweep.
+os.environ.setdefault("OMP_WAIT_POLICY", "PASSIVE")
 REF_DIR = os.path.join(HERE, "_ref")
 _LIB = None
 
@@ -51,6 +54,11 @@ def lib():
         L.or_v2_solve.argtypes = [ctypes.c_int, u32p, u16p, ctypes.c_int, ctypes.c_int, u16p,
                                   ctypes.c_uint64, u64p, u64p, u8p, u64p, u64p, ctypes.c_int,
                                   ctypes.c_int]
+        L.or_v1_init.restype = ctypes.c_uint64
+        L.or_v1_init.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, u16p, ctypes.c_uint64, u8p]
+        L.or_v1_sweep_slice.restype = ctypes.c_uint64
+        L.or_v1_sweep_slice.argtypes = [ctypes.c_int, u32p, u16p, ctypes.c_int, ctypes.c_int, u64p, u64p,
+                                        u8p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int]
         L.or_verdict.restype = ctypes.c_int64
         L.or_verdict.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.c_int, u8p,
                                  ctypes.POINTER(ctypes.c_int)]
@@ -153,6 +161,32 @@ def solve_v2(graph, k: int, p: int, threads: int = 0, max_passes: int = 4096) ->
                    [int(x) for x in counts[:passes]])
     _verdict(sol)
     return sol
+
+
+class SweepSample:
+    """The CPU baseline's unit of work: one v1 pass (every column, k_cops_visibility.cpp:146-291)
+    over a slice of the configurations, on a freshly initialised table."""
+
+    def __init__(self, graph, k: int, p: int = 1):
+        L = lib()
+        self.graph, self.k, self.p = graph, k, p
+        self.cfg = configs(graph.n, k)
+        self.heads, self.trans = transitions(graph, k, self.cfg)
+        self.row_ptr, col = graph.csr()
+        self.col = np.ascontiguousarray(col if col.size else np.zeros(1, np.uint16))
+        self.count = self.cfg.shape[0]
+        self.states = np.empty(self.count * graph.n * 2 * p, dtype=np.uint8)
+        L.or_v1_init(graph.n, k, p, _p(self.cfg, u16p), self.count, _p(self.states, u8p))
+
+    @property
+    def total_states(self) -> int:
+        return self.count * self.graph.n * 2 * self.p
+
+    def run(self, c0: int, c1: int, threads: int = 0) -> int:
+        tr = self.trans if self.trans.size else np.zeros(1, np.uint64)
+        return int(lib().or_v1_sweep_slice(self.graph.n, _p(self.row_ptr, u32p), _p(self.col, u16p), self.k,
+                                           self.p, _p(self.heads, u64p), _p(tr, u64p), _p(self.states, u8p),
+                                           c0, c1, threads))
 
 
 def _verdict(sol: Solution) -> None:

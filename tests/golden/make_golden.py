@@ -71,6 +71,34 @@ def record(path: str, name: str, k: int, p: int, solver: str, timeout: float) ->
     return case
 
 
+def large() -> None:
+    """The large single solve's digests (minutes of CPU time; run with --large):
+    n=255 by the reference binary itself (its format stops at 255 vertices), and the n=256
+    product configuration by the oracle's C restatement, pinned by the n=255 agreement."""
+
+    out = {}
+    src = os.path.join(HERE, "graphs", "regular4_n255_s12345.txt")
+    c = record(src, "regular4_n255_s12345", 3, 1, "k_cops_visibility", 7200)
+    c["matrix"] = os.path.relpath(src, HERE)
+    c["pinned_by"] = "reference binary"
+    out["n255"] = c
+    g = G.load_matrix(os.path.join(HERE, "graphs", "regular4_n256_s12345.txt"))
+    t0 = time.time()
+    sol = O.solve_v1(g, 3, 1)
+    out["n256"] = {
+        "graph": "regular4_n256_s12345", "matrix": "graphs/regular4_n256_s12345.txt", "k": 3, "p": 1,
+        "solver": "k_cops_visibility", "n": 256, "columns": 2, "config_count": int(sol.configs.shape[0]),
+        "pass_counts": sol.pass_counts, "base_captures": sol.base_captures,
+        "result": "WIN" if sol.win else "LOSS", "sha_states": sha(sol.states.tobytes()),
+        "sha_heads": sha(sol.heads.tobytes()), "sha_transitions": sha(sol.transitions.tobytes()),
+        "n_transitions": int(sol.transitions.size), "pinned_by": "oracle (C restatement)",
+        "oracle_seconds": round(time.time() - t0, 1),
+    }
+    with open(os.path.join(HERE, "large.json"), "w") as f:
+        json.dump(out, f, indent=1)
+    print("wrote large.json")
+
+
 def main() -> None:
     os.makedirs(OUT_MATRICES, exist_ok=True)
     if not O.ref_available():
@@ -116,4 +144,7 @@ def main() -> None:
 
 
 if __name__ == "__main__":
-    main()
+    if "--large" in sys.argv:
+        large()
+    else:
+        main()

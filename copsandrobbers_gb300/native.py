@@ -94,6 +94,9 @@ SIGNATURES = {
     "cr_solve": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(CrGraph), ctypes.c_int32, ctypes.c_int32,
                                 ctypes.c_int32, c_u8p, ctypes.c_size_t, c_u64p, ctypes.c_int32, c_i32p,
                                 ctypes.POINTER(CrVerdict), ctypes.POINTER(CrSolveStats)]),
+    "cr_solve_v1_noalloc": (ctypes.c_int, [ctypes.POINTER(CrGraph), ctypes.c_int32, ctypes.c_int32,
+                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, c_u64p,
+                                           ctypes.c_int32, c_i32p, c_u64p, ctypes.c_char_p, ctypes.c_size_t]),
 }
 
 _lib = None

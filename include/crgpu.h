@@ -149,6 +149,29 @@ int cr_solve(cr_context* ctx, const cr_graph* g, int32_t k, int32_t p, int32_t r
              uint8_t* states_out, size_t states_bytes, uint64_t* pass_counts, int32_t cap,
              int32_t* passes, cr_verdict* verdict, cr_solve_stats* stats);
 
+/* ---- allocation-free solve ------------------------------------------------------------ */
+
+/* No counterpart in the reference.  The v1 solve (loadGraphFile..mainLoop) for callers that
+ * cannot allocate memory -- a caller working inside a memory pool or budget it does not own,
+ * one that must not take the CUDA allocator's locks on its critical path, or an embedder that
+ * forbids libraries from owning device memory.  The caller passes the graph as host arrays
+ * and the states table as device memory it owns (states_bytes >= C(n+k-1,k) * n * 2p); all
+ * other working memory is one fixed 64 MiB __device__ array inside the library, so nothing is
+ * allocated: no cudaMalloc/cudaFree, no pinned host memory, no streams, events or graphs.
+ *   - Limit: n <= 512 and a working set (everything but the table) within 64 MiB, e.g.
+ *     n=128 with k=3 at p=1; larger solves return CR_ERR_LIMIT with the bytes needed in err.
+ *   - Every GPU that loads the library holds the 64 MiB until the process exits.
+ *   - The first call on a device looks up the array's device address (once per device);
+ *     make it before any stream capture on that device.
+ *   - All calls share the array and leave their contents in it; each call clears what must
+ *     start at zero.  Calls whose GPU work overlaps (other streams or host threads) race.
+ * stream: cudaStream_t or NULL.  pass_counts[0 .. *passes) receive the per-pass counts;
+ * err (may be NULL) receives a message on failure. */
+int cr_solve_v1_noalloc(const cr_graph* g, int32_t k, int32_t p, void* stream,
+                        uint8_t* states_dev, size_t states_bytes, uint64_t* pass_counts,
+                        int32_t cap, int32_t* passes, uint64_t* base_captures, char* err,
+                        size_t err_len);
+
 #ifdef __cplusplus
 }
 #endif

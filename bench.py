@@ -146,6 +146,69 @@ def cpu_baseline(graph, k: int, p: int, passes: int, budget_s: float = 20.0) -> 
                       f"({swept} states, {t_total:.1f} s), scaled by the solve's {passes} passes"}
 
 
+def batched_workload(ctx, count: int = 4096, plain_sample: int = 128) -> dict:
+    """Cop numbers of `count` seeded connected G(n, p) graphs, n ~ U[16, 128], mean degree
+    ~ U[3, 6], k = 1, 2, 3 in order: one persistent launch (cr_batch_solve) against the plain
+    form -- one solve per (graph, k) through the public API -- timed on an evenly spaced sample
+    of the graphs and checked table by table (digests and pass-count hashes)."""
+    import numpy as np
+
+    from copsandrobbers_gb300 import graphs as G
+    from copsandrobbers_gb300 import native as N
+    from copsandrobbers_gb300.solver import Solver, batch_solve, solver_digest
+
+    rng = np.random.default_rng(2024)
+    graphs = [G.erdos_renyi(int(rng.integers(16, 129)), float(rng.uniform(3, 6)),
+                            G.sub_seed(2024, i) & 0xFFFFFFFF) for i in range(count)]
+    batch_solve(ctx, graphs[:64], 3, 1, 0)  # warm-up (and autotune)
+    out = batch_solve(ctx, graphs, 3, 1, 0)
+    batched = out.stats.states / (out.stats.ms / 1e3)
+    sample = list(range(0, count, max(1, count // plain_sample)))
+    t0 = time.perf_counter()
+    states, mismatch = 0, 0
+    for gi in sample:
+        for k in range(1, 4):
+            r = out.results[gi][k - 1]
+            if not r["solved"]:
+                break
+            with Solver(ctx, graphs[gi], k, 1) as s:
+                s.init()
+                cnt = s.run()
+                dg = solver_digest(s)
+            states += int(r["states"])
+            mismatch += int(dg != r["digest"] or N.pass_hash(cnt) != r["pass_hash"])
+    plain = states / (time.perf_counter() - t0)
+    return {"workload": f"{count} connected G(n,p), n~U[16,128], mean degree~U[3,6], k=1..3 until WIN",
+            "batched_states_per_s": batched, "plain_states_per_s": plain,
+            "batched_over_plain": batched / plain, "batched_ms": out.stats.ms,
+            "states": int(out.stats.states), "ctas": int(out.stats.ctas), "threads": int(out.stats.threads),
+            "plain_sample_graphs": len(sample), "table_mismatches": mismatch,
+            "cop_number_histogram": [int(x) for x in np.bincount(out.cop_numbers, minlength=4)]}
+
+
+def limited_visibility_workload(ctx) -> dict:
+    """v2 rules on the seeded Delaunay-thinned graph, n=199, mean degree 4.5, k=2, p=3."""
+    from copsandrobbers_gb300 import graphs as G
+    from copsandrobbers_gb300 import native as N
+    from copsandrobbers_gb300.solver import Solver
+
+    g = G.delaunay_thinned(199, 2024)
+    with Solver(ctx, g, 2, 3, N.CR_RULES_V2) as s:
+        s.init()
+        s.run()
+        s.init()
+        t0 = time.perf_counter()
+        counts = s.run()
+        dt = time.perf_counter() - t0
+        v = s.verdict()
+        st = s.stats()
+        S = int(s.sizes().num_states)
+    return {"workload": "Delaunay-thinned n=199 (seed 2024, mean degree 4.5), k=2, p=3, v2 rules",
+            "states": S, "solve_s": dt, "states_per_s": S / dt, "passes": len(counts),
+            "device_ms": st.main_ms, "verdict": "WIN" if v.win else "LOSS",
+            "reference": "the reference v2 solver did not finish this graph at p=2 within 600 s"}
+
+
 def run_reference(args) -> None:
     rank, world, _ = dist_info()
     if rank != 0:
@@ -299,6 +362,10 @@ def run_gpu(args) -> None:
     e2e_value = S * args.steps * world / (e2e_ms / 1e3)
 
     line = None
+    extra = {}
+    if rank == 0 and not args.headline_only:
+        extra["batched"] = batched_workload(ctx)
+        extra["limited_visibility"] = limited_visibility_workload(ctx)
     if rank == 0:
         base = cpu_baseline(g, k, p, passes) if not args.no_cpu_baseline else None
         line = {
@@ -319,6 +386,7 @@ def run_gpu(args) -> None:
             "clocks": clocks.summary(),
             "gpu_launches": launches_per_step * args.steps,
         }
+        line.update(extra)
         print(json.dumps(line), flush=True)
     ctx.close()
     if world > 1:
@@ -332,6 +400,8 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="skip the batched and limited-visibility workloads")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

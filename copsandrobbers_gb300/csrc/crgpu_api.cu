@@ -12,6 +12,7 @@
 
 #include "../../include/crgpu.h"
 #include "crgpu_internal.cuh"
+#include "crgpu_ctx.h"
 #include "crgpu_v2.h"
 
 namespace crgpu {
@@ -34,18 +35,10 @@ void launch_trans(int k, const uint16_t* configs, uint32_t C, int n, const uint3
                   const unsigned long long* heads, unsigned long long* data, unsigned int* err,
                   int grid, cudaStream_t st);
 void launch_scan(const unsigned long long* in, unsigned long long* out, uint32_t C, cudaStream_t st);
+void launch_digest(const uint8_t* table, size_t bytes, unsigned long long* out, int grid, cudaStream_t st);
 }  // namespace crgpu
 
 using namespace crgpu;
-
-struct cr_context {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    int num_sms = 1;
-    bool profiling = false;
-    std::string err;
-};
 
 // Per-solve state.  Host copies of the graph are kept for the hop masks and file output.
 struct cr_solver {
@@ -72,6 +65,7 @@ struct cr_solver {
     uint16_t* d_rcol = nullptr;
     uint32_t* d_nbr = nullptr;
     uint32_t* d_iso = nullptr;
+    uint32_t* d_rhop = nullptr;
     ColMeta* d_meta = nullptr;
     unsigned long long* d_counters = nullptr;  // [0] pass_new, [1] verdict key, [2] scratch
     unsigned int* d_err = nullptr;
@@ -222,7 +216,7 @@ uint64_t cr_solver_footprint(int32_t n, int32_t k, int32_t p, int32_t rules) {
     b += C * S * rwp * 4 + C;                            // push-mode candidate rows and flags
     b += (uint64_t)cols * C;                             // flags
     b += C * (uint64_t)k * 2;                            // configs
-    b += (uint64_t)n * rwp * 4 + (uint64_t)k * (n + 1) * 4 + (1u << 16);
+    b += (uint64_t)n * rwp * 4 * 3 + (uint64_t)k * (n + 1) * 4 + (1u << 16);
     return b;
 }
 
@@ -231,14 +225,14 @@ static void free_v1(cr_solver* s) {
     s->pass_graph = nullptr;
     void* ptrs[] = {s->d_rp, s->d_col, s->d_binom, s->d_configs, s->d_hop, s->d_table,
                     s->d_marked, s->d_front, s->d_fflag, s->d_meta, s->d_counters, s->d_err,
-                    s->d_heads, s->d_trans, s->d_cand, s->d_cflag, s->d_rrp, s->d_rcol, s->d_nbr, s->d_iso};
+                    s->d_heads, s->d_trans, s->d_cand, s->d_cflag, s->d_rrp, s->d_rcol, s->d_nbr, s->d_iso, s->d_rhop};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     s->d_rp = nullptr; s->d_col = nullptr; s->d_binom = nullptr; s->d_configs = nullptr;
     s->d_hop = nullptr; s->d_table = nullptr; s->d_marked = nullptr; s->d_front = nullptr;
     s->d_fflag = nullptr; s->d_meta = nullptr; s->d_counters = nullptr; s->d_err = nullptr;
     s->d_heads = nullptr; s->d_trans = nullptr; s->d_cand = nullptr; s->d_cflag = nullptr;
-    s->d_rrp = nullptr; s->d_rcol = nullptr; s->d_nbr = nullptr; s->d_iso = nullptr;
+    s->d_rrp = nullptr; s->d_rcol = nullptr; s->d_nbr = nullptr; s->d_iso = nullptr; s->d_rhop = nullptr;
     if (s->h_pinned) cudaFreeHost(s->h_pinned);
     s->h_pinned = nullptr;
     cudaEvent_t evs[] = {s->ev0, s->ev1, s->evc0, s->evc1};
@@ -258,6 +252,7 @@ static V1Dev dev_view(const cr_solver* s) {
     d.g.rcol = s->d_rcol;
     d.g.nbr = s->d_nbr;
     d.g.isolated = s->d_iso;
+    d.g.rhop = s->d_rhop;
     d.g.maxdeg = s->maxdeg;
     d.k = s->k;
     d.cols = s->cols;
@@ -313,6 +308,14 @@ static int alloc_v1(cr_solver* s) {
     CR_CUDA(ctx, cudaMalloc(&s->d_hop, (size_t)s->n * s->rwp * 4));
     std::vector<uint32_t> hop = hop_masks(s);
     CR_CUDA(ctx, cudaMemcpyAsync(s->d_hop, hop.data(), hop.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+    // transposed hop masks: bit r of row u iff u in hop(r)
+    std::vector<uint32_t> rhop(hop.size(), 0);
+    for (int r = 0; r < s->n; ++r)
+        for (int u = 0; u < s->n; ++u)
+            if ((hop[(size_t)r * s->rwp + (u >> 5)] >> (u & 31)) & 1u)
+                rhop[(size_t)u * s->rwp + (r >> 5)] |= 1u << (r & 31);
+    CR_CUDA(ctx, cudaMalloc(&s->d_rhop, rhop.size() * 4));
+    CR_CUDA(ctx, cudaMemcpyAsync(s->d_rhop, rhop.data(), rhop.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
     // out-neighbour masks (capture-seed closed form) and the in-neighbour CSR (push mode)
     std::vector<uint32_t> nbr((size_t)s->n * s->rwp, 0);
     std::vector<uint32_t> rrp(s->n + 1, 0);
@@ -708,6 +711,20 @@ int cr_solver_stats(cr_solver* s, cr_solve_stats* out) {
 
 static const uint8_t* table_ptr(const cr_solver* s) {
     return s->rules == CR_RULES_V1 ? s->d_table : crgpu::v2_table(s->v2);
+}
+
+int cr_solver_digest(cr_solver* s, uint64_t* digest) {
+    if (!s || !digest) return CR_ERR_INVALID;
+    cr_context* ctx = s->ctx;
+    CR_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    CR_CUDA(ctx, cudaMemsetAsync(s->d_counters + 2, 0, sizeof(unsigned long long), st));
+    launch_digest(table_ptr(s), s->C * (size_t)s->n * s->cols, s->d_counters + 2, ctx->num_sms * 4, st);
+    CR_CUDA(ctx, cudaGetLastError());
+    CR_CUDA(ctx, cudaMemcpyAsync(s->h_pinned + 2, s->d_counters + 2, 8, cudaMemcpyDeviceToHost, st));
+    CR_CUDA(ctx, cudaStreamSynchronize(st));
+    *digest = s->h_pinned[2];
+    return CR_OK;
 }
 
 int cr_solver_device_states(cr_solver* s, void** dev_ptr, size_t* bytes) {

@@ -52,6 +52,7 @@ struct DevGraph {
     const uint16_t* rcol;
     const uint32_t* nbr;      // [n][rwp]: out-neighbour masks
     const uint32_t* isolated; // [rwp]: vertices without out-neighbours
+    const uint32_t* rhop;     // [n][rwp]: bit r of row u set iff u is in hop(r) (transposed hop)
 };
 
 // Everything one v1 solve's kernels touch.

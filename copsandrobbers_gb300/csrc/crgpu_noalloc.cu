@@ -77,8 +77,8 @@ int scratch_base(int device, unsigned char** out, char* err, size_t err_len) {
 
 // Byte offsets of every buffer inside the scratch area (256-byte aligned).
 struct Layout {
-    size_t rp, col, rrp, rcol, cursor, nbr, iso, hop, binom, configs, marked, front, fflag, cand,
-        cflag, meta, counters, err, total;
+    size_t rp, col, rrp, rcol, cursor, nbr, iso, hop, rhop, binom, configs, marked, front, fflag,
+        cand, cflag, meta, counters, err, total;
 };
 
 Layout plan(int n, size_t nnz, int k, int cols, uint64_t C, int rwp, int S) {
@@ -98,6 +98,7 @@ Layout plan(int n, size_t nnz, int k, int cols, uint64_t C, int rwp, int S) {
     L.nbr = take((size_t)n * rwp * 4);
     L.iso = take((size_t)rwp * 4);
     L.hop = take((size_t)n * rwp * 4);
+    L.rhop = take((size_t)n * rwp * 4);
     L.binom = take((size_t)k * (n + 1) * 4);
     L.configs = take(C * k * 2);
     L.marked = take((size_t)cols * C * rwp * 4);
@@ -188,6 +189,19 @@ __global__ void k_na_hop(const uint32_t* nbr, int n, int rwp, int p, uint32_t* h
     }
 }
 
+// Transposed hop masks: bit r of row u iff u is in hop(r).
+__global__ void k_na_rhop(const uint32_t* hop, int n, int rwp, uint32_t* rhop) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
+        for (int w = 0; w < rwp; ++w) {
+            uint32_t b = hop[(size_t)r * rwp + w];
+            while (b) {
+                const int u = w * 32 + __ffs(b) - 1;
+                b &= b - 1;
+                atomicOr(&rhop[(size_t)u * rwp + (r >> 5)], 1u << (r & 31));
+            }
+        }
+}
+
 int fail(char* err, size_t err_len, int code, const char* msg) {
     if (err && err_len) snprintf(err, err_len, "%s", msg);
     return code;
@@ -261,6 +275,7 @@ extern "C" int cr_solve_v1_noalloc(const cr_graph* g, int32_t k, int32_t p, void
         d.g.rcol = reinterpret_cast<const uint16_t*>(base + L.rcol);
         d.g.nbr = reinterpret_cast<const uint32_t*>(base + L.nbr);
         d.g.isolated = reinterpret_cast<const uint32_t*>(base + L.iso);
+        d.g.rhop = reinterpret_cast<const uint32_t*>(base + L.rhop);
         int maxdeg = 0;
         for (int v = 0; v < n; ++v) maxdeg = maxdeg > (int)(g->row_ptr[v + 1] - g->row_ptr[v]) ? maxdeg : (int)(g->row_ptr[v + 1] - g->row_ptr[v]);
         d.g.maxdeg = maxdeg;
@@ -291,6 +306,7 @@ extern "C" int cr_solve_v1_noalloc(const cr_graph* g, int32_t k, int32_t p, void
         k_na_scan<<<1, 1, 0, st>>>(cursor, reinterpret_cast<uint32_t*>(base + L.rrp), n);
         k_na_fill<<<4, 256, 0, st>>>(d.g.row_ptr, d.g.col, n, cursor, reinterpret_cast<uint16_t*>(base + L.rcol));
         k_na_hop<<<4, 128, 0, st>>>(d.g.nbr, n, rwp, p, reinterpret_cast<uint32_t*>(base + L.hop));
+        k_na_rhop<<<4, 128, 0, st>>>(d.hop, n, rwp, reinterpret_cast<uint32_t*>(base + L.rhop));
         launch_unrank(d.binom, n, k, (uint32_t)C, reinterpret_cast<uint16_t*>(base + L.configs),
                       gsmall > 0 ? gsmall : 1, st);
         NA_CUDA(cudaGetLastError());

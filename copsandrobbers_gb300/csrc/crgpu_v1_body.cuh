@@ -1,0 +1,803 @@
+// crgpu_v1_body.cuh - device bodies of the v1 frontier kernels (see crgpu_v1.cu for the
+// algorithm).  Each body runs on `nwk` workers (thread blocks) of which this block is `wk`:
+// the stand-alone kernels pass (blockIdx.x, gridDim.x); the persistent batch kernel, where one
+// block owns a whole solve, passes (0, 1) and separates the bodies with __syncthreads.
+//
+// The including file defines CR_BODY_NS (the namespace of this instance), CR_LDG (a load of
+// data that does not change while the kernel runs), CR_RESTRICT and CR_BODY_INLINE.  Inside the persistent
+// batch kernel a block writes the very buffers it later reads (and reuses them job after job),
+// so there both are plain coherent loads; the stand-alone kernels use the read-only path.
+#pragma once
+#include "crgpu_internal.cuh"
+
+namespace crgpu {
+namespace CR_BODY_NS {
+
+
+#define FULL_MASK 0xFFFFFFFFu
+#define CR_MAX_K_DEV 4
+
+// Lexicographic rank of a sorted multiset (see config_rank): B read through CR_LDG, or from
+// shared memory when staged there.
+template <int K>
+__device__ __forceinline__ uint32_t rank_g(const int (&c)[K], const uint32_t* B, int np1) {
+    uint32_t r = 0;
+    int prev = 0;
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+        r += CR_LDG(&B[i * np1 + prev]) - CR_LDG(&B[i * np1 + c[i]]);
+        prev = c[i];
+    }
+    return r;
+}
+template <int K>
+__device__ __forceinline__ uint32_t rank_s(const int (&c)[K], const uint32_t* sB, int np1) {
+    uint32_t r = 0;
+    int prev = 0;
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+        r += sB[i * np1 + prev] - sB[i * np1 + c[i]];
+        prev = c[i];
+    }
+    return r;
+}
+
+// Shared-memory words of one lane group of the last-column body.
+__host__ __device__ inline int and_group_words(int S, int rwp) { return 3 * rwp + S * rwp; }
+
+// Words of shared memory the pull body stages the rank table in (16-byte multiple).
+__host__ __device__ inline int rank_table_words(int k, int n) { return (k * (n + 1) + 3) & ~3; }
+
+__device__ __forceinline__ bool frontier_sparse(const ColMeta& m, uint32_t C) {
+    return (unsigned long long)m.rows * kPushRatio < C;
+}
+
+// Per-warp running totals a producer reports once at the end of its grid-stride loop.
+struct Tally {
+    unsigned cnt = 0, err = 0, rows = 0;
+    int lo = kEmptyLo, hi = -1;
+
+    __device__ void flush(const V1Dev& d, int col, int lane) {
+        cnt = __reduce_add_sync(FULL_MASK, cnt);
+        rows = __reduce_add_sync(FULL_MASK, rows);
+        lo = __reduce_min_sync(FULL_MASK, lo);
+        hi = __reduce_max_sync(FULL_MASK, hi);
+        err = __reduce_or_sync(FULL_MASK, err);
+        if (lane == 0) {
+            if (cnt) atomicAdd(d.pass_new, (unsigned long long)cnt);
+            if (rows) atomicAdd(&d.meta[col].rows, (int)rows);
+            if (hi >= 0) {
+                atomicMin(&d.meta[col].lo, lo);
+                atomicMax(&d.meta[col].hi, hi);
+            }
+            if (err) atomicOr(d.err, err);
+        }
+    }
+};
+
+// Before a producer run of column `col` (whose inputs are column nx): fix the value base of
+// its output frontier, reset the range, and clear the frontier flags -- unless the column is
+// in append mode (column 0 in pass 1, whose frontier already holds the capture seeds).
+__device__ CR_BODY_INLINE void prep_body(const V1Dev& d, int col, int nx, unsigned wk, unsigned nwk) {
+    ColMeta* mo = d.meta + col;
+    const int append = mo->append;
+    if (wk == 0 && threadIdx.x == 0) {
+        if (!append) {
+            const ColMeta mi = d.meta[nx];
+            mo->base = (mi.hi >= mi.lo) ? mi.lo + 1 : 0;
+            mo->lo = kEmptyLo;
+            mo->hi = -1;
+            mo->rows = 0;
+        }
+        mo->seed = 0;
+        if (col == 0) *d.pass_new = 0ull;
+        if (col == d.cols - 1) d.meta[0].append = 0;  // column 0's seeded frontier is consumed
+    }
+    if (!append) {
+        uint8_t* f = d.fflag + (size_t)col * d.C;
+        for (size_t i = (size_t)wk * blockDim.x + threadIdx.x; i < d.C;
+             i += (size_t)nwk * blockDim.x)
+            f[i] = 0;
+    }
+}
+
+// initializeCaptures (k_cops_visibility.cpp:85-127): the table was memset to 0xFE; a robber
+// on a cop is a capture of round 0 in columns 0 and 1 only.  The seeds also form the first
+// frontiers of columns 0 and 1 (value 0, slot 0); their rows are written whole.
+__device__ CR_BODY_INLINE void init_body(const V1Dev& d, int K, unsigned wk, unsigned nwk) {
+    unsigned caps = 0;
+    const int n = d.g.n, rwp = d.g.rwp, S = d.S;
+    for (uint32_t cid = wk * blockDim.x + threadIdx.x; cid < d.C;
+         cid += nwk * blockDim.x) {
+        const uint16_t* cc = d.configs + (size_t)cid * K;
+        int wi[CR_MAX_K_DEV];
+        uint32_t bi[CR_MAX_K_DEV];
+        int nb = 0, prev = -1;
+        for (int i = 0; i < K; ++i) {
+            const int r = cc[i];
+            if (r == prev) continue;
+            prev = r;
+            wi[nb] = r >> 5;
+            bi[nb] = 1u << (r & 31);
+            ++nb;
+            const size_t cell = ((size_t)cid * n + r) * d.cols;
+            d.table[cell] = 1;
+            d.table[cell + 1] = 1;
+        }
+        caps += nb;
+        // the seed rows of columns 0 and 1: marked rows and slot 0 of the frontier rows,
+        // written whole (the other slots zero) with 16-byte stores where rows allow it
+        uint32_t* rows[4] = {d.marked + (size_t)cid * rwp, d.marked + ((size_t)d.C + cid) * rwp,
+                             d.front + (size_t)cid * S * rwp, d.front + ((size_t)d.C + cid) * S * rwp};
+        const int len[4] = {rwp, rwp, S * rwp, S * rwp};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            for (int w0 = 0; w0 < len[q]; w0 += 4) {
+                uint32_t x[4];
+                for (int j = 0; j < 4; ++j) {
+                    x[j] = 0u;
+                    for (int b = 0; b < nb; ++b)
+                        if (wi[b] == w0 + j) x[j] |= bi[b];
+                }
+                if ((rwp & 3) == 0) {
+                    *reinterpret_cast<uint4*>(rows[q] + w0) = make_uint4(x[0], x[1], x[2], x[3]);
+                } else {
+                    for (int j = 0; j < 4 && w0 + j < len[q]; ++j) rows[q][w0 + j] = x[j];
+                }
+            }
+        }
+        d.fflag[cid] = 1;
+        d.fflag[(size_t)d.C + cid] = 1;
+    }
+    caps = __reduce_add_sync(FULL_MASK, caps);
+    if ((threadIdx.x & 31) == 0 && caps) atomicAdd(d.pass_new, (unsigned long long)caps);
+}
+
+// ---- lane groups ---------------------------------------------------------------------
+// A warp works on CPW = 32 / G configurations at once, G lanes per configuration (G >= rwp,
+// so every word of a robber row has its own lane).  All lanes of a warp run the same control
+// flow over the same number of rounds (groups without work are predicated off), so warp-wide
+// shuffles and ballots stay legal, and the loads of CPW rows are in flight together.
+template <int G>
+struct Lanes {
+    int lane, glane, grp;
+    unsigned gmask;
+    __device__ explicit Lanes(int l)
+        : lane(l), glane(l & (G - 1)), grp(l / G),
+          gmask(G == 32 ? FULL_MASK : (((1u << G) - 1u) << ((l / G) * G))) {}
+    __device__ bool any(bool p) const { return (__ballot_sync(FULL_MASK, p) & gmask) != 0u; }
+    __device__ bool all(bool p) const { return (__ballot_sync(FULL_MASK, p) & gmask) == gmask; }
+    __device__ int sum(int v) const {
+#pragma unroll
+        for (int off = G / 2; off >= 1; off >>= 1) v += __shfl_xor_sync(FULL_MASK, v, off);
+        return v;
+    }
+};
+
+// Mark the states of row cid in column col from wacc = OR of the successors' frontier
+// rows (slot s <-> value base_in + s): the lowest slot with a bit gives 1 + min.  Writes the
+// table bytes, the marked row, the output frontier row and flag.  All lanes of the warp call
+// it; `valid` is the group's predicate.
+template <int G>
+__device__ __forceinline__ void emit_row(const V1Dev& d, uint32_t cid, bool valid, int col, uint32_t m,
+                                         const uint32_t* wacc, uint32_t* wnew, int base_in,
+                                         int s_used, int out_base, int append, const Lanes<G>& L,
+                                         Tally& t) {
+    const int n = d.g.n, rw = d.g.rw, rwp = d.g.rwp, S = d.S;
+    const int gl = L.glane;
+    const uint32_t vm = (valid && gl < rw) ? valid_mask(n, gl) : 0u;
+    uint32_t mm = m, any = 0;
+    if (valid && gl < rw) {
+        for (int s = 0; s < s_used; ++s) {
+            const int v = base_in + s + 1;
+            const uint32_t nb = (v < kMaxRound) ? (wacc[s * rwp + gl] & ~mm & vm) : 0u;
+            mm |= nb;
+            wnew[s * rwp + gl] = nb;
+            any |= nb;
+            if (nb) {
+                t.lo = min(t.lo, v);
+                t.hi = max(t.hi, v);
+                const int so = v - out_base;
+                if (so < 0 || so >= S) t.err |= kErrSlot;
+            }
+        }
+    }
+    __syncwarp();
+    if (L.any(any != 0)) {
+        if (gl < rw) {
+            d.marked[((size_t)col * d.C + cid) * rwp + gl] = mm;
+            t.cnt += __popc(mm ^ m);
+        }
+        // column 0's frontier is consumed only through its flags and range (the last column
+        // reads column 0's marked row and table bytes), so its rows are not stored
+        if (col != 0) {
+            uint32_t* frow = d.front + ((size_t)col * d.C + cid) * S * rwp;
+            for (int e = gl; e < S * rwp; e += G) {
+                const int so = e / rwp, w = e - so * rwp;
+                const int s = out_base + so - base_in - 1;
+                const uint32_t val = (s >= 0 && s < s_used && w < rw) ? wnew[s * rwp + w] : 0u;
+                frow[e] = append ? (frow[e] | val) : val;
+            }
+        }
+        if (gl == 0) {
+            d.fflag[(size_t)col * d.C + cid] = 1;
+            t.rows++;
+        }
+        // table bytes: each lane walks the new bits of its own word (slots are disjoint)
+        if (gl < rw) {
+            uint8_t* trow = d.table + ((size_t)cid * n + gl * 32) * d.cols + col;
+            for (int s = 0; s < s_used; ++s) {
+                uint32_t b = wnew[s * rwp + gl];
+                const uint8_t val = (uint8_t)(1 | ((base_in + s + 1) << 1));
+                while (b) {
+                    trow[(size_t)(__ffs(b) - 1) * d.cols] = val;
+                    b &= b - 1;
+                }
+            }
+        }
+    }
+    __syncwarp();
+}
+
+// OR-reduce NWP per-lane words across the G lanes of a group by recursive halving: at each
+// step a lane keeps one half of its words and receives the partner's copy of that half.
+// The group's reduced row lands in out[0 .. nwords).
+template <int NWP, int G>
+__device__ __forceinline__ void group_or(uint32_t (&acc)[NWP], int gl, uint32_t* out, int nwords) {
+    constexpr int STEPS = (NWP < G ? NWP : G) == 1 ? 0 : __builtin_ctz(NWP < G ? NWP : G);
+    constexpr int R = NWP >= G ? NWP / G : 1;
+    int w = 0;
+    int lb = G >> 1;
+#pragma unroll
+    for (int st = 0; st < STEPS; ++st) {
+        const int half = NWP >> (st + 1);
+        const bool up = (gl & lb) != 0;
+#pragma unroll
+        for (int i = 0; i < NWP / 2; ++i) {
+            if (i < half) {
+                const uint32_t send = up ? acc[i] : acc[i + half];
+                const uint32_t keep = up ? acc[i + half] : acc[i];
+                acc[i] = keep | __shfl_xor_sync(FULL_MASK, send, lb);
+            }
+        }
+        if (up) w += half;
+        lb >>= 1;
+    }
+    // lanes left sharing the same words (NWP < G)
+    for (; lb >= 1; lb >>= 1) acc[0] |= __shfl_xor_sync(FULL_MASK, acc[0], lb);
+    const bool writer = NWP >= G || (gl & ((G / NWP) - 1)) == 0;
+    if (writer) {
+#pragma unroll
+        for (int i = 0; i < R; ++i)
+            if (w + i < nwords) out[w + i] = acc[i];
+    }
+}
+
+// Dense cop turn: a lane group per configuration.  Each lane takes its own successor tuples
+// (one rank per tuple), ORs whole frontier rows of the flagged successors into NWP per-lane
+// words, and the group reduces them by halving.
+template <int K, int NWP, int G>
+__device__ CR_BODY_INLINE void cop_pull_body(const V1Dev& d, int col, int nx, unsigned wk, unsigned nwk) {
+    extern __shared__ uint32_t sm[];
+    constexpr int CPW = 32 / G;
+    constexpr int U = 4;  // successor tuples in flight per lane
+    const int warp = threadIdx.x >> 5;
+    const Lanes<G> L(threadIdx.x & 31);
+    const int gl = L.glane;
+    const int n = d.g.n, rw = d.g.rw, rwp = d.g.rwp, S = d.S;
+    const ColMeta mi = d.meta[nx];
+    if (mi.hi < mi.lo) return;                              // empty frontier: nothing changes
+    if (mi.seed || frontier_sparse(mi, d.C)) return;       // the seed or push form handles it
+    const int base_in = mi.base;
+    const int s_used = min(mi.hi - base_in + 1, S);
+    const int nwords = s_used * rwp;
+    const int out_base = d.meta[col].base;
+    const int append = d.meta[col].append;
+    const int np1 = n + 1;
+    // the rank table lives in shared memory for the whole body
+    uint32_t* sB = sm;
+    for (int i = threadIdx.x; i < K * np1; i += blockDim.x) sB[i] = CR_LDG(&d.binom[i]);
+    __syncthreads();
+    uint32_t* wacc = sm + rank_table_words(K, n) + (warp * CPW + L.grp) * (2 * S * rwp);
+    uint32_t* wnew = wacc + S * rwp;
+    const uint32_t* CR_RESTRICT fin = d.front + (size_t)nx * d.C * S * rwp;
+    const uint8_t* CR_RESTRICT fflag_in = d.fflag + (size_t)nx * d.C;
+    const uint32_t* CR_RESTRICT rp = d.g.row_ptr;
+    const uint16_t* CR_RESTRICT adj = d.g.col;
+    const bool vec4 = (rwp & 3) == 0;
+    Tally t;
+    const size_t step = (size_t)nwk * (blockDim.x >> 5) * CPW;
+    for (size_t cb = ((size_t)wk * (blockDim.x >> 5) + warp) * CPW; cb < d.C; cb += step) {
+        const uint32_t cid = (uint32_t)(cb + L.grp);
+        const bool ok = cid < d.C;
+        const uint32_t vm = (ok && gl < rw) ? valid_mask(n, gl) : 0u;
+        const uint32_t m = (ok && gl < rw) ? d.marked[((size_t)col * d.C + cid) * rwp + gl] : 0u;
+        const bool full = L.all(m == vm);                 // every lane votes (no short circuit)
+        const bool need = ok && !full;                    // some robber position still open
+        if (!__any_sync(FULL_MASK, need)) continue;
+        int lo[K], dg[K];
+        int T = 0;
+        if (need) {
+            const uint16_t* cc = d.configs + (size_t)cid * K;
+            T = 1;
+#pragma unroll
+            for (int i = 0; i < K; ++i) {
+                const int v = cc[i];
+                lo[i] = CR_LDG(&rp[v]);
+                dg[i] = CR_LDG(&rp[v + 1]) - lo[i];
+                T *= dg[i];
+            }
+        }
+        {
+            uint32_t acc[NWP];
+#pragma unroll
+            for (int i = 0; i < NWP; ++i) acc[i] = 0u;
+            const int Tmax = __reduce_max_sync(FULL_MASK, T);
+            // odometer over N(c_0) x ... x N(c_{K-1}), last index fastest: this lane starts at
+            // tuple gl and steps by G (one division per configuration, not per tuple)
+            int idx[K];
+            {
+                int rem = T > 0 ? gl : 0;
+#pragma unroll
+                for (int i = K - 1; i >= 0; --i) {
+                    const int q = dg[i] > 0 ? rem / dg[i] : 0;
+                    idx[i] = rem - q * dg[i];
+                    rem = q;
+                }
+            }
+            for (int t0 = 0; t0 < Tmax; t0 += G * U) {
+                uint32_t s[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    s[u] = 0xFFFFFFFFu;
+                    if (t0 + u * G + gl < T) {
+                        int c[K];
+#pragma unroll
+                        for (int i = 0; i < K; ++i) c[i] = CR_LDG(&adj[lo[i] + idx[i]]);
+                        sort_small<K>(c);
+                        s[u] = rank_s<K>(c, sB, np1);
+                        int carry = G;
+#pragma unroll
+                        for (int i = K - 1; i >= 0; --i) {
+                            if (!carry) break;
+                            const int v = idx[i] + carry;
+                            if (i == 0 || v < dg[i]) { idx[i] = v; carry = 0; }
+                            else if (v < 2 * dg[i]) { idx[i] = v - dg[i]; carry = 1; }
+                            else { carry = v / dg[i]; idx[i] = v - carry * dg[i]; }
+                        }
+                    }
+                }
+                unsigned live = 0;
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    if (s[u] == 0xFFFFFFFFu) continue;
+                    if (s[u] >= d.C) { t.err |= kErrRank; continue; }
+                    if (CR_LDG(&fflag_in[s[u]])) live |= 1u << u;
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    if (!((live >> u) & 1u)) continue;
+                    const uint32_t* row = fin + (size_t)s[u] * S * rwp;
+                    if (vec4) {
+#pragma unroll
+                        for (int w = 0; w < NWP; w += 4) {
+                            if (w < nwords) {
+                                const uint4 x = CR_LDG(reinterpret_cast<const uint4*>(row + w));
+                                acc[w] |= x.x; acc[w + 1] |= x.y; acc[w + 2] |= x.z; acc[w + 3] |= x.w;
+                            }
+                        }
+                    } else {
+#pragma unroll
+                        for (int w = 0; w < NWP; ++w)
+                            if (w < nwords) acc[w] |= CR_LDG(row + w);
+                    }
+                }
+            }
+            group_or<NWP, G>(acc, gl, wacc, need ? nwords : 0);
+        }
+        __syncwarp();
+        emit_row<G>(d, cid, need, col, m, wacc, wnew, base_in, s_used, out_base, append, L, t);
+    }
+    t.flush(d, col, L.lane);
+}
+
+// Cop turn from the capture seeds (column 1 before pass 1): OR over T(C) of the seed rows
+// {r : r in C'} is the union of the cops' neighbourhoods (empty if a cop has no move), so no
+// successor is visited.  All seed values are 0: one slot.
+template <int K, int G>
+__device__ CR_BODY_INLINE void cop_seed_body(const V1Dev& d, int col, int nx, unsigned wk, unsigned nwk) {
+    extern __shared__ uint32_t sm[];
+    constexpr int CPW = 32 / G;
+    const int warp = threadIdx.x >> 5;
+    const Lanes<G> L(threadIdx.x & 31);
+    const int gl = L.glane;
+    const int n = d.g.n, rw = d.g.rw, rwp = d.g.rwp, S = d.S;
+    const ColMeta mi = d.meta[nx];
+    if (!mi.seed || mi.hi < mi.lo) return;
+    const int out_base = d.meta[col].base;
+    const int append = d.meta[col].append;
+    uint32_t* wacc = sm + (warp * CPW + L.grp) * (2 * S * rwp);
+    uint32_t* wnew = wacc + S * rwp;
+    const uint32_t* CR_RESTRICT rp = d.g.row_ptr;
+    Tally t;
+    const size_t step = (size_t)nwk * (blockDim.x >> 5) * CPW;
+    for (size_t cb = ((size_t)wk * (blockDim.x >> 5) + warp) * CPW; cb < d.C; cb += step) {
+        const uint32_t cid = (uint32_t)(cb + L.grp);
+        const bool ok = cid < d.C;
+        const uint32_t vm = (ok && gl < rw) ? valid_mask(n, gl) : 0u;
+        const uint32_t m = (ok && gl < rw) ? d.marked[((size_t)col * d.C + cid) * rwp + gl] : 0u;
+        const bool full = L.all(m == vm);
+        const bool need = ok && !full;
+        if (!__any_sync(FULL_MASK, need)) continue;
+        if (need && gl < rwp) {
+            const uint16_t* cc = d.configs + (size_t)cid * K;
+            uint32_t x = 0;
+            bool moves = true;
+#pragma unroll
+            for (int i = 0; i < K; ++i) {
+                const int v = cc[i];
+                moves &= CR_LDG(&rp[v + 1]) > CR_LDG(&rp[v]);
+                x |= CR_LDG(&d.g.nbr[(size_t)v * rwp + gl]);
+            }
+            wacc[gl] = moves ? x : 0u;
+        }
+        __syncwarp();
+        emit_row<G>(d, cid, need, col, m, wacc, wnew, mi.base, 1, out_base, append, L, t);
+    }
+    t.flush(d, col, L.lane);
+}
+
+// Sparse cop turn, scatter: every non-empty frontier row of column nx is ORed into the
+// candidate rows of its predecessors (the product of the cops' in-neighbour lists).
+template <int K>
+__device__ CR_BODY_INLINE void cop_push_body(const V1Dev& d, int col, int nx, unsigned wk, unsigned nwk) {
+    extern __shared__ uint32_t sm[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n = d.g.n, rwp = d.g.rwp, S = d.S;
+    const ColMeta mi = d.meta[nx];
+    if (mi.hi < mi.lo || mi.seed || !frontier_sparse(mi, d.C)) return;
+    const int s_used = min(mi.hi - mi.base + 1, S);
+    const int nwords = s_used * rwp;
+    uint32_t* wrow = sm + warp * (S * rwp);
+    const uint32_t* CR_RESTRICT fin = d.front + (size_t)nx * d.C * S * rwp;
+    const uint8_t* CR_RESTRICT fflag_in = d.fflag + (size_t)nx * d.C;
+    const uint32_t* CR_RESTRICT rrp = d.g.rrow_ptr;
+    const uint16_t* CR_RESTRICT radj = d.g.rcol;
+    const int np1 = n + 1;
+    unsigned err = 0;
+    const size_t stride = (size_t)nwk * blockDim.x;
+    for (size_t base = (size_t)wk * blockDim.x + warp * 32; base < d.C; base += stride) {
+        const size_t mine = base + lane;
+        unsigned act = __ballot_sync(FULL_MASK, mine < d.C && fflag_in[mine]);
+        while (act) {
+            const uint32_t cp = (uint32_t)(base + __ffs(act) - 1);
+            act &= act - 1;
+            const uint32_t* row = fin + (size_t)cp * S * rwp;
+            uint32_t nz = 0;
+            for (int e = lane; e < nwords; e += 32) {
+                wrow[e] = row[e];
+                if (wrow[e]) nz = 1;
+            }
+            const bool any = __any_sync(FULL_MASK, nz != 0);
+            __syncwarp();
+            if (any) {
+                const uint16_t* cc = d.configs + (size_t)cp * K;
+                int lo[K], dg[K];
+                int T = 1;
+#pragma unroll
+                for (int i = 0; i < K; ++i) {
+                    const int v = cc[i];
+                    lo[i] = CR_LDG(&rrp[v]);
+                    dg[i] = CR_LDG(&rrp[v + 1]) - lo[i];
+                    T *= dg[i];
+                }
+                for (int tt = lane; tt < T; tt += 32) {
+                    int c[K];
+                    int rem = tt;
+#pragma unroll
+                    for (int i = K - 1; i >= 0; --i) {
+                        const int q = rem / dg[i];
+                        c[i] = CR_LDG(&radj[lo[i] + rem - q * dg[i]]);
+                        rem = q;
+                    }
+                    sort_small<K>(c);
+                    const uint32_t pc = rank_g<K>(c, d.binom, np1);
+                    if (pc >= d.C) { err |= kErrRank; continue; }
+                    uint32_t* crow = d.cand + (size_t)pc * S * rwp;
+                    for (int e = 0; e < nwords; ++e)
+                        if (wrow[e]) atomicOr(&crow[e], wrow[e]);
+                    d.cflag[pc] = 1;
+                }
+            }
+            __syncwarp();
+        }
+    }
+    err = __reduce_or_sync(FULL_MASK, err);
+    if (lane == 0 && err) atomicOr(d.err, err);
+}
+
+// The flagged configurations of a 32-configuration window, CPW at a time: group g takes the
+// g-th remaining flag.  Returns the group's config (valid = false when fewer remain).
+template <int G>
+__device__ __forceinline__ uint32_t take_flagged(unsigned& act, size_t base, const Lanes<G>& L,
+                                                 bool& valid) {
+    constexpr int CPW = 32 / G;
+    const unsigned pos = __fns(act, 0, L.grp + 1);
+    valid = pos < 32u;
+#pragma unroll
+    for (int i = 0; i < CPW; ++i) act &= act - 1;  // (a no-op once act is empty)
+    return valid ? (uint32_t)(base + pos) : 0u;
+}
+
+// Sparse cop turn, mark: the configurations that received candidates; their candidate rows
+// are consumed and cleared for the next push.
+template <int G>
+__device__ CR_BODY_INLINE void cop_apply_body(const V1Dev& d, int col, int nx, unsigned wk, unsigned nwk) {
+    extern __shared__ uint32_t sm[];
+    constexpr int CPW = 32 / G;
+    const int warp = threadIdx.x >> 5;
+    const Lanes<G> L(threadIdx.x & 31);
+    const int gl = L.glane;
+    const int rw = d.g.rw, rwp = d.g.rwp, S = d.S;
+    const ColMeta mi = d.meta[nx];
+    if (mi.hi < mi.lo || mi.seed || !frontier_sparse(mi, d.C)) return;
+    const int base_in = mi.base;
+    const int s_used = min(mi.hi - base_in + 1, S);
+    const int out_base = d.meta[col].base;
+    const int append = d.meta[col].append;
+    uint32_t* wacc = sm + (warp * CPW + L.grp) * (2 * S * rwp);
+    uint32_t* wnew = wacc + S * rwp;
+    Tally t;
+    const size_t stride = (size_t)nwk * blockDim.x;
+    for (size_t base = (size_t)wk * blockDim.x + warp * 32; base < d.C; base += stride) {
+        const size_t mine = base + L.lane;
+        unsigned act = __ballot_sync(FULL_MASK, mine < d.C && d.cflag[mine]);
+        while (act) {
+            bool valid;
+            const uint32_t cid = take_flagged<G>(act, base, L, valid);
+            uint32_t m = 0;
+            if (valid) {
+                uint32_t* crow = d.cand + (size_t)cid * S * rwp;
+                for (int e = gl; e < S * rwp; e += G) {
+                    wacc[e] = crow[e];
+                    crow[e] = 0u;
+                }
+                if (gl == 0) d.cflag[cid] = 0;
+                if (gl < rw) m = d.marked[((size_t)col * d.C + cid) * rwp + gl];
+            }
+            __syncwarp();
+            emit_row<G>(d, cid, valid, col, m, wacc, wnew, base_in, s_used, out_base, append, L, t);
+        }
+    }
+    t.flush(d, col, L.lane);
+}
+
+// Deferred robber turn (odd column below the last): (C, r, c) = 1 + (C, r, c+1), row-local.
+template <int G>
+__device__ CR_BODY_INLINE void direct_body(const V1Dev& d, int col, int nx, unsigned wk, unsigned nwk) {
+    extern __shared__ uint32_t sm[];
+    constexpr int CPW = 32 / G;
+    const int warp = threadIdx.x >> 5;
+    const Lanes<G> L(threadIdx.x & 31);
+    const int gl = L.glane;
+    const int rw = d.g.rw, rwp = d.g.rwp, S = d.S;
+    const ColMeta mi = d.meta[nx];
+    if (mi.hi < mi.lo) return;
+    const int base_in = mi.base;
+    const int s_used = min(mi.hi - base_in + 1, S);
+    const int out_base = d.meta[col].base;
+    const int append = d.meta[col].append;
+    uint32_t* wacc = sm + (warp * CPW + L.grp) * (2 * S * rwp);
+    uint32_t* wnew = wacc + S * rwp;
+    const uint8_t* CR_RESTRICT fflag_in = d.fflag + (size_t)nx * d.C;
+    Tally t;
+    const size_t stride = (size_t)nwk * blockDim.x;
+    for (size_t base = (size_t)wk * blockDim.x + warp * 32; base < d.C; base += stride) {
+        const size_t mine = base + L.lane;
+        unsigned act = __ballot_sync(FULL_MASK, mine < d.C && fflag_in[mine]);
+        while (act) {
+            bool valid;
+            const uint32_t cid = take_flagged<G>(act, base, L, valid);
+            uint32_t m = 0;
+            if (valid) {
+                const uint32_t* row = d.front + ((size_t)nx * d.C + cid) * S * rwp;
+                for (int e = gl; e < S * rwp; e += G) wacc[e] = e < s_used * rwp ? row[e] : 0u;
+                if (gl < rw) m = d.marked[((size_t)col * d.C + cid) * rwp + gl];
+            }
+            __syncwarp();
+            emit_row<G>(d, cid, valid, col, m, wacc, wnew, base_in, s_used, out_base, append, L, t);
+        }
+    }
+    t.flush(d, col, L.lane);
+}
+
+// Last column (robber move cashed out over the exact-p-hop cloud) from column 0.
+// A lane group per configuration whose column-0 row changed; the work is row-local.  Three
+// forms per row, whichever touches the fewest vertices:
+//   touch (few column-0 marks): only an r whose hop(r) meets the marked row can be complete
+//          (or an r with empty hop(r)); those are the OR of the transposed hop rows of the
+//          marked vertices, and only they are tested;
+//   block (few column-0 vertices unmarked): the open r that some unmarked u blocks are the OR
+//          of the transposed hop rows of those u; every other open r is complete;
+//   test  (few open r): every open r tests hop(r) within column 0's marked row.
+// Only the states found complete read column 0's table bytes (for the max).
+template <bool P1, int G>
+__device__ CR_BODY_INLINE void and_body(const V1Dev& d, int col, unsigned wk, unsigned nwk) {
+    extern __shared__ uint32_t sm[];
+    constexpr int CPW = 32 / G;
+    const int warp = threadIdx.x >> 5;
+    const Lanes<G> L(threadIdx.x & 31);
+    const int gl = L.glane;
+    const int n = d.g.n, rw = d.g.rw, rwp = d.g.rwp, S = d.S, cols = d.cols;
+    const ColMeta mi = d.meta[0];
+    if (mi.hi < mi.lo) return;
+    const int out_base = d.meta[col].base;
+    const int per_grp = and_group_words(S, rwp);
+    uint32_t* wm0 = sm + (warp * CPW + L.grp) * per_grp;
+    uint32_t* wmc = wm0 + rwp;
+    uint32_t* wtouch = wmc + rwp;
+    uint32_t* wnew = wtouch + rwp;
+    const uint8_t* CR_RESTRICT fflag0 = d.fflag;
+    const uint32_t* CR_RESTRICT rp = d.g.row_ptr;
+    const uint16_t* CR_RESTRICT adj = d.g.col;
+    const int avg_deg = max(1, (int)((CR_LDG(&rp[n]) + n - 1) / n));
+    Tally t;
+    const size_t stride = (size_t)nwk * blockDim.x;
+    for (size_t base = (size_t)wk * blockDim.x + warp * 32; base < d.C; base += stride) {
+        const size_t mine = base + L.lane;
+        unsigned act = __ballot_sync(FULL_MASK, mine < d.C && fflag0[mine]);
+        while (act) {
+            bool valid;
+            const uint32_t cid = take_flagged<G>(act, base, L, valid);
+            uint32_t* mrow = d.marked + ((size_t)col * d.C + cid) * rwp;
+            const uint32_t vm = (valid && gl < rw) ? valid_mask(n, gl) : 0u;
+            const uint32_t mc = (valid && gl < rw) ? mrow[gl] : 0u;
+            const bool full = L.all(mc == vm);            // every lane votes (no short circuit)
+            const bool need = valid && !full;
+            if (!__any_sync(FULL_MASK, need)) continue;
+            const uint32_t m0 = (need && gl < rw) ? d.marked[(size_t)cid * rwp + gl] : 0u;
+            if (need && gl < rwp) {
+                wm0[gl] = m0;
+                wmc[gl] = mc;
+            }
+            if (need)
+                for (int e = gl; e < S * rwp; e += G) wnew[e] = 0u;
+            const int marked0 = L.sum(__popc(m0));
+            const int open = L.sum(__popc(~mc & vm));
+            const int c_test = open * (P1 ? avg_deg : rw);
+            const int c_block = (n - marked0) * rwp;
+            const int c_touch = marked0 * rwp + (P1 ? marked0 * avg_deg : open);
+            const bool touch_form = c_touch < c_test && c_touch <= c_block;
+            const bool block_form = !touch_form && c_block < c_test;
+            if (__any_sync(FULL_MASK, touch_form && need)) {
+                // each lane ORs the transposed hop rows of the marked vertices in its own word;
+                // the group reduces the rows by halving into wtouch
+                uint32_t acc[G];
+#pragma unroll
+                for (int i = 0; i < G; ++i) acc[i] = 0u;
+                if (touch_form && need && gl < rw) {
+                    uint32_t mb = m0;
+                    while (mb) {
+                        const int v = gl * 32 + __ffs(mb) - 1;
+                        mb &= mb - 1;
+                        const uint32_t* row = d.g.rhop + (size_t)v * rwp;
+#pragma unroll
+                        for (int w = 0; w < G; ++w)
+                            if (w < rwp) acc[w] |= CR_LDG(&row[w]);
+                    }
+                }
+                group_or<G, G>(acc, gl, wtouch, (touch_form && need) ? rwp : 0);
+            }
+            __syncwarp();
+            if (need && gl < rw) {
+                const uint8_t* trow = d.table + (size_t)cid * n * cols;
+                // candidates: touched and open (count form), open and not blocked (block form,
+                // all of them complete), or every open state (test form)
+                uint32_t cand = ~mc & vm;
+                if (touch_form) cand &= wtouch[gl] | CR_LDG(&d.g.isolated[gl]);
+                if (block_form) {
+                    uint32_t blocked = 0;
+                    for (int w2 = 0; w2 < rw; ++w2) {
+                        uint32_t ub = ~wm0[w2] & valid_mask(n, w2);
+                        while (ub) {
+                            const int u = w2 * 32 + __ffs(ub) - 1;
+                            ub &= ub - 1;
+                            blocked |= CR_LDG(&d.g.rhop[(size_t)u * rwp + gl]);
+                        }
+                    }
+                    cand &= ~blocked;
+                }
+                while (cand) {
+                    const int r = gl * 32 + __ffs(cand) - 1;
+                    cand &= cand - 1;
+                    const uint32_t e0 = CR_LDG(&rp[r]), e1 = CR_LDG(&rp[r + 1]);
+                    bool all;
+                    int mx = 0;
+                    if (P1) {
+                        if (block_form) {
+                            all = true;
+                        } else {
+                            all = true;
+                            for (uint32_t e = e0; e < e1 && all; ++e) {
+                                const int v = CR_LDG(&adj[e]);
+                                all = (wm0[v >> 5] >> (v & 31)) & 1u;
+                            }
+                        }
+                        if (all)
+                            for (uint32_t e = e0; e < e1; ++e)
+                                mx = max(mx, (int)(trow[(size_t)CR_LDG(&adj[e]) * cols] >> 1));
+                    } else {
+                        const uint32_t* h = d.hop + (size_t)r * rwp;
+                        all = true;
+                        if (!block_form)
+                            for (int w = 0; w < rw && all; ++w) all = (CR_LDG(&h[w]) & ~wm0[w]) == 0u;
+                        if (all) {
+                            for (int w = 0; w < rw; ++w) {
+                                uint32_t b = CR_LDG(&h[w]);
+                                while (b) {
+                                    const int v = w * 32 + __ffs(b) - 1;
+                                    b &= b - 1;
+                                    mx = max(mx, (int)(trow[(size_t)v * cols] >> 1));
+                                }
+                            }
+                        }
+                    }
+                    if (!all) continue;
+                    const int v = mx + 1;
+                    if (v >= kMaxRound) continue;
+                    const int so = v - out_base;
+                    if (so < 0 || so >= S) { t.err |= kErrSlot; continue; }
+                    wnew[so * rwp + gl] |= 1u << (r & 31);  // this lane owns word r >> 5
+                    d.table[((size_t)cid * n + r) * cols + col] = (uint8_t)(1 | (v << 1));
+                    t.lo = min(t.lo, v);
+                    t.hi = max(t.hi, v);
+                }
+            }
+            __syncwarp();
+            uint32_t nb = 0;
+            if (need && gl < rw)
+                for (int s = 0; s < S; ++s) nb |= wnew[s * rwp + gl];
+            if (L.any(nb != 0)) {
+                if (gl < rw) {
+                    mrow[gl] = mc | nb;
+                    t.cnt += __popc(nb);
+                }
+                uint32_t* frow = d.front + ((size_t)col * d.C + cid) * S * rwp;
+                for (int e = gl; e < S * rwp; e += G) frow[e] = wnew[e];
+                if (gl == 0) {
+                    d.fflag[(size_t)col * d.C + cid] = 1;
+                    t.rows++;
+                }
+            }
+            __syncwarp();
+        }
+    }
+    t.flush(d, col, L.lane);
+}
+
+// findFinalResult (k_cops_visibility.cpp:301-331): key = worst << 32 | cid, minimised, is the
+// first config (lowest id) among those with the strictly smallest worst case.  Each lane
+// tests one config's column-0 row; the warp then scans the bytes of the complete rows.
+__device__ CR_BODY_INLINE void verdict_body(const uint8_t* table, const uint32_t* m0, uint32_t C,
+                                             int n, int rw, int rwp, int cols,
+                                             unsigned long long* best, unsigned wk, unsigned nwk) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const size_t stride = (size_t)nwk * blockDim.x;
+    for (size_t base = (size_t)wk * blockDim.x + warp * 32; base < C; base += stride) {
+        const size_t cid = base + lane;
+        bool full = cid < C;
+        for (int w = 0; w < rw && full; ++w) full = m0[cid * rwp + w] == valid_mask(n, w);
+        unsigned act = __ballot_sync(FULL_MASK, full);
+        while (act) {
+            const size_t c = base + __ffs(act) - 1;
+            act &= act - 1;
+            int wc = 0;
+            for (int r = lane; r < n; r += 32) wc = max(wc, (int)(table[(c * n + r) * cols] >> 1));
+            wc = __reduce_max_sync(FULL_MASK, wc);
+            if (lane == 0) atomicMin(best, ((unsigned long long)wc << 32) | c);
+        }
+    }
+}
+
+}  // namespace CR_BODY_NS
+}  // namespace crgpu

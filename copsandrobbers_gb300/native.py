@@ -49,14 +49,29 @@ class CrSolveStats(ctypes.Structure):
                 ("slots", ctypes.c_int32), ("resolved", ctypes.c_uint64)]
 
 
-class CrBatchJob(ctypes.Structure):
-    _fields_ = [("graph", CrGraph), ("k", ctypes.c_int32), ("p", ctypes.c_int32)]
-
-
 class CrBatchResult(ctypes.Structure):
-    _fields_ = [("status", ctypes.c_int32), ("passes", ctypes.c_int32),
-                ("verdict", CrVerdict), ("states", ctypes.c_uint64),
-                ("base_captures", ctypes.c_uint64), ("table_digest", ctypes.c_uint64)]
+    _fields_ = [("solved", ctypes.c_int32), ("status", ctypes.c_int32), ("win", ctypes.c_int32),
+                ("capture_plies", ctypes.c_int32), ("passes", ctypes.c_int32), ("pad", ctypes.c_int32),
+                ("best_config", ctypes.c_int64), ("base_captures", ctypes.c_uint64),
+                ("states", ctypes.c_uint64), ("digest", ctypes.c_uint64), ("pass_hash", ctypes.c_uint64)]
+
+
+class CrBatchStats(ctypes.Structure):
+    _fields_ = [("ms", ctypes.c_double), ("states", ctypes.c_uint64), ("ctas", ctypes.c_int32),
+                ("threads", ctypes.c_int32), ("slot_bytes", ctypes.c_int64)]
+
+
+class CrRequestResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("win", ctypes.c_int32), ("capture_plies", ctypes.c_int32),
+                ("passes", ctypes.c_int32), ("best_config", ctypes.c_int64), ("base_captures", ctypes.c_uint64),
+                ("states", ctypes.c_uint64), ("digest", ctypes.c_uint64), ("pass_hash", ctypes.c_uint64),
+                ("queue_ms", ctypes.c_double), ("run_ms", ctypes.c_double), ("latency_ms", ctypes.c_double)]
+
+
+class CrServerStats(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_uint64) for f in ("completed", "failed", "queued", "running", "max_running",
+                                               "memory_budget", "memory_in_use", "peak_memory_in_use",
+                                               "states_done")] + [("busy_ms", ctypes.c_double)]
 
 
 class CrGpuError(RuntimeError):
@@ -94,6 +109,19 @@ SIGNATURES = {
     "cr_solve": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(CrGraph), ctypes.c_int32, ctypes.c_int32,
                                 ctypes.c_int32, c_u8p, ctypes.c_size_t, c_u64p, ctypes.c_int32, c_i32p,
                                 ctypes.POINTER(CrVerdict), ctypes.POINTER(CrSolveStats)]),
+    "cr_batch_solve": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(CrGraph), ctypes.c_int32, ctypes.c_int32,
+                                      ctypes.c_int32, ctypes.c_int32, c_i32p, ctypes.POINTER(CrBatchResult),
+                                      ctypes.POINTER(CrBatchStats)]),
+    "cr_solver_digest": (ctypes.c_int, [ctypes.c_void_p, c_u64p]),
+    "cr_server_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_uint64, ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]),
+    "cr_server_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(CrGraph), ctypes.c_int32, ctypes.c_int32,
+                                        ctypes.c_int32, c_u64p]),
+    "cr_server_poll": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32, ctypes.POINTER(CrRequestResult)]),
+    "cr_server_read_states": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, c_u8p, ctypes.c_size_t]),
+    "cr_server_release": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
+    "cr_server_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(CrServerStats)]),
+    "cr_server_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+    "cr_server_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "cr_solve_v1_noalloc": (ctypes.c_int, [ctypes.POINTER(CrGraph), ctypes.c_int32, ctypes.c_int32,
                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, c_u64p,
                                            ctypes.c_int32, c_i32p, c_u64p, ctypes.c_char_p, ctypes.c_size_t]),
@@ -116,6 +144,43 @@ def lib():
             fn.argtypes = args
         _lib = L
     return _lib
+
+
+MASK64 = (1 << 64) - 1
+
+
+def mix64(z: int) -> int:
+    """splitmix64 finaliser (the mixer of the table digest)."""
+    z &= MASK64
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & MASK64
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & MASK64
+    return z ^ (z >> 31)
+
+
+def table_digest(table) -> int:
+    """The digest cr_solver_digest computes, restated with numpy (tables of any length)."""
+    import numpy as np
+
+    b = np.ascontiguousarray(table, dtype=np.uint8).ravel()
+    pad = (-b.size) % 8
+    if pad:
+        b = np.concatenate([b, np.zeros(pad, np.uint8)])
+    w = b.view("<u8").astype(np.uint64)
+    j = np.arange(w.size, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        z = w ^ (j * np.uint64(0x9E3779B97F4A7C15))
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+        return int(z.sum(dtype=np.uint64))
+
+
+def pass_hash(counts) -> int:
+    """The pass-count hash of a batch result: sum_i mix64(count_i ^ (i * 0xD1B54A32D192ED03))."""
+    h = 0
+    for i, c in enumerate(counts, start=1):
+        h = (h + mix64(int(c) ^ ((i * 0xD1B54A32D192ED03) & MASK64))) & MASK64
+    return h
 
 
 def declared_symbols() -> list[str]:

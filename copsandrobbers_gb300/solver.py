@@ -219,3 +219,30 @@ def parse_matrix(text: bytes) -> Graph:
     for v in range(n.value):
         adj[v, col[rp[v]:rp[v + 1]]] = 1
     return Graph(adj)
+
+
+@dataclass
+class BatchOutput:
+    cop_numbers: list            # per graph: first winning k, 0 = none up to kmax
+    results: list                # per graph, per k: dict of the cr_batch_result fields
+    stats: N.CrBatchStats
+
+
+def batch_solve(ctx: Context, graphs: list, kmax: int = 3, p: int = 1, threads: int = 0) -> BatchOutput:
+    """Cop numbers of many graphs in one persistent launch (cr_batch_solve)."""
+    keep = [_GraphArgs(g) for g in graphs]
+    arr = (N.CrGraph * len(graphs))(*[k.struct for k in keep])
+    cop = (ctypes.c_int32 * len(graphs))()
+    res = (N.CrBatchResult * (len(graphs) * kmax))()
+    st = N.CrBatchStats()
+    _check(ctx.ptr, N.lib().cr_batch_solve(ctx.ptr, arr, len(graphs), kmax, p, threads, cop, res,
+                                           ctypes.byref(st)))
+    fields = [f for f, _ in N.CrBatchResult._fields_ if f != "pad"]
+    out = [[{f: getattr(res[g * kmax + i], f) for f in fields} for i in range(kmax)] for g in range(len(graphs))]
+    return BatchOutput([int(c) for c in cop], out, st)
+
+
+def solver_digest(s: Solver) -> int:
+    d = ctypes.c_uint64()
+    _check(s.ctx.ptr, N.lib().cr_solver_digest(s.ptr, ctypes.byref(d)))
+    return int(d.value)

@@ -149,6 +149,91 @@ int cr_solve(cr_context* ctx, const cr_graph* g, int32_t k, int32_t p, int32_t r
              uint8_t* states_out, size_t states_bytes, uint64_t* pass_counts, int32_t cap,
              int32_t* passes, cr_verdict* verdict, cr_solve_stats* stats);
 
+/* ---- batches of small solves ----------------------------------------------------------- */
+
+/* One (graph, k) solve of a batch.  The reference has no batched mode; each entry is what one
+ * run of solvers/k_cops_visibility.cpp on that graph and k would report. */
+typedef struct cr_batch_result {
+    int32_t solved;          /* 1 = this k was solved (0: a smaller k already won) */
+    int32_t status;          /* CR_OK or the device error of this solve */
+    int32_t win;
+    int32_t capture_plies;
+    int32_t passes;          /* mainLoop passes, the final empty one included */
+    int32_t pad;
+    int64_t best_config;
+    uint64_t base_captures;
+    uint64_t states;         /* C(n+k-1, k) * n * 2p */
+    uint64_t digest;         /* cr_solver_digest of the table */
+    uint64_t pass_hash;      /* sum_i mix64(count_i ^ (i * 0xD1B54A32D192ED03)), i = 1.. */
+} cr_batch_result;
+
+typedef struct cr_batch_stats {
+    double ms;               /* device time of the batch launch (CUDA events) */
+    uint64_t states;         /* states of every solved (graph, k) */
+    int32_t ctas;            /* persistent thread blocks */
+    int32_t threads;         /* threads per block */
+    int64_t slot_bytes;      /* device memory per block */
+} cr_batch_stats;
+
+/* Cop numbers of many graphs (v1 rules, visibility p): for every graph, k = 1..kmax in
+ * order, stopping at the first WIN, all in one persistent launch.  cop_number[g] = first
+ * winning k or 0; results[g * kmax + k - 1] per solve.  threads_per_cta = 0 lets an autotuner
+ * pick the launch shape (cached per device and batch shape).  n <= 128, kmax <= 3, p = 1. */
+int cr_batch_solve(cr_context* ctx, const cr_graph* graphs, int32_t count, int32_t kmax, int32_t p,
+                   int32_t threads_per_cta, int32_t* cop_number, cr_batch_result* results,
+                   cr_batch_stats* stats);
+
+/* 64-bit digest of a solver's states table: sum over its 8-byte little-endian words w_j
+ * (zero-padded) of mix64(w_j ^ (j * 0x9E3779B97F4A7C15)) modulo 2^64, mix64 being the
+ * splitmix64 finaliser.  Used to compare batched and single solves without copying tables. */
+int cr_solver_digest(cr_solver* s, uint64_t* digest);
+
+/* ---- solve server ---------------------------------------------------------------------- */
+
+/* A long-running solve service (the reference has no counterpart: it answers one solve per
+ * process run).  Requests queue as they arrive; worker threads, each with its own stream,
+ * start the first queued request whose device footprint (cr_solver_footprint) fits in the
+ * memory budget left, so requests arriving while others run are admitted as soon as a worker
+ * and memory free up and their solves overlap on the GPU.  Finished tables stay resident
+ * until cr_server_release.  A queued request waiting more than 2 s is not overtaken. */
+typedef struct cr_server cr_server;
+
+typedef struct cr_request_result {
+    int32_t status;          /* CR_OK or the solve's error code */
+    int32_t win;
+    int32_t capture_plies;
+    int32_t passes;
+    int64_t best_config;
+    uint64_t base_captures;
+    uint64_t states;
+    uint64_t digest;         /* cr_solver_digest of the table */
+    uint64_t pass_hash;      /* as in cr_batch_result */
+    double queue_ms;         /* submit -> start */
+    double run_ms;           /* start -> done */
+    double latency_ms;       /* submit -> done */
+} cr_request_result;
+
+typedef struct cr_server_report {
+    uint64_t completed, failed, queued, running, max_running;
+    uint64_t memory_budget, memory_in_use, peak_memory_in_use;
+    uint64_t states_done;
+    double busy_ms;          /* first submit -> last completion */
+} cr_server_report;
+
+/* memory_budget = 0: 80% of the device memory free at creation. */
+int cr_server_create(int32_t device, uint64_t memory_budget, int32_t workers, cr_server** out);
+/* Copies the graph; CR_ERR_NOMEM if the request could never fit the budget. */
+int cr_server_submit(cr_server* srv, const cr_graph* g, int32_t k, int32_t p, int32_t rules,
+                     uint64_t* request_id);
+/* wait_ms: 0 = do not wait, < 0 = wait until done.  CR_ERR_STATE while queued or running. */
+int cr_server_poll(cr_server* srv, uint64_t request_id, int32_t wait_ms, cr_request_result* out);
+int cr_server_read_states(cr_server* srv, uint64_t request_id, uint8_t* dst, size_t bytes);
+/* Frees a finished request's resident table and returns its memory to the budget. */
+int cr_server_release(cr_server* srv, uint64_t request_id);
+int cr_server_stats(cr_server* srv, cr_server_report* out);
+const char* cr_server_last_error(const cr_server* srv);
+int cr_server_destroy(cr_server* srv);
+
 /* ---- allocation-free solve ------------------------------------------------------------ */
 
 /* No counterpart in the reference.  The v1 solve (loadGraphFile..mainLoop) for callers that

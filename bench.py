@@ -12,8 +12,9 @@ to the fixed point (every pass, with its host read of the pass count).  The stat
   value   resolved states/s = S * steps / device time, CUDA events on the solver's stream
   e2e     the same metric through the public C ABI call cr_solve() from host CSR arrays in
           pinned memory to the states table back in pinned host memory, every step
-  roofline  the cop-turn kernel (the dominant one): algorithmic bytes per launch / mean
-          launch time (CUDA events around each launch in a separate profiled solve)
+  roofline  the dominant kernel, k_init_pass1 (initializeCaptures and pass 1 in one sweep):
+          algorithmic bytes per launch / its CUDA-event time; "solve" gives the whole solve's
+          algorithmic state-store bytes / device time per solve
   cpu_baseline  the oracle's C restatement of the reference sweep on all host cores, timed on
           a bounded sample (one pass over a slice of the configurations), scaled to a solve
 
@@ -112,8 +113,8 @@ def measured_peak_hbm() -> tuple[float, str]:
 
 
 def traffic_per_launch() -> float | None:
-    """DRAM bytes per cop-turn launch from the committed ncu summary, if present."""
-    path = os.path.join(ROOT, "profiles", "k_cop_large_n256.md")
+    """DRAM bytes per k_init_pass1 launch from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "k_init_pass1_large_n256.md")
     try:
         for line in open(path):
             if line.startswith("traffic_bytes_per_launch:"):
@@ -207,6 +208,32 @@ def limited_visibility_workload(ctx) -> dict:
             "states": S, "solve_s": dt, "states_per_s": S / dt, "passes": len(counts),
             "device_ms": st.main_ms, "verdict": "WIN" if v.win else "LOSS",
             "reference": "the reference v2 solver did not finish this graph at p=2 within 600 s"}
+
+
+def serving_workload(count: int, rate: float, workers: int = 8) -> dict:
+    """A seeded Poisson stream of solve requests through the solve server (cr_server_*):
+    4-regular / G(n, 4/(n-1)) / Delaunay-thinned graphs, n log-uniform in [20, 400], k in
+    {1, 2, 3}, 10% with visibility period p in [2, 4]; admission by device footprint, tables
+    resident until the client releases them."""
+    from copsandrobbers_gb300.serving import Server, request_stream, run_stream
+
+    t0 = time.perf_counter()
+    reqs = request_stream(count, rate_per_s=rate, seed=12)
+    gen_s = time.perf_counter() - t0
+    with Server(0, 0, workers=workers) as srv:
+        run_stream(srv, request_stream(40, rate_per_s=1e6, seed=99))   # warm-up
+        out = run_stream(srv, reqs)
+    failed = sum(1 for r in out["results"] if r["status"] != 0)
+    lat_q = sorted(float(r["queue_ms"]) for r in out["results"])
+    return {"workload": f"{count} Poisson arrivals at {rate:g} requests/s (seed 12): 4-regular / "
+                        "G(n,p) mean degree 4 / Delaunay-thinned, n log-uniform in [20,400], k in {1,2,3}, "
+                        "10% with p in [2,4]",
+            "rate_per_s": rate, "requests": count, "workers": workers, "wall_s": out["wall_s"],
+            "p50_ms": out["p50_ms"], "p99_ms": out["p99_ms"], "mean_ms": out["mean_ms"],
+            "queue_p50_ms": lat_q[len(lat_q) // 2] if lat_q else None,
+            "states": out["states"], "states_per_s": out["states_per_s"], "failed": failed,
+            "max_running": out["stats"]["max_running"],
+            "peak_memory_in_use": out["stats"]["peak_memory_in_use"], "generate_s": gen_s}
 
 
 def run_reference(args) -> None:
@@ -303,24 +330,31 @@ def run_gpu(args) -> None:
     value = S * args.steps * world / (ms / 1e3)
     verdict = solver.verdict()
 
-    # roofline: time each cop-turn launch in one profiled solve
-    ctx.set_profiling(True)
+    # roofline of the dominant kernel, k_init_pass1 (initializeCaptures and pass 1 in one
+    # sweep): its launch time comes from CUDA events around it on the solver's stream
+    # (stats.init_ms) in one further solve after the timed region
     solver.init()
     solver.run()
     st = solver.stats()
-    ctx.set_profiling(False)
-    cop_launches = int(st.cop_step_launches)
-    mean_ms = st.cop_step_ms / max(cop_launches, 1)
     C, n = int(sizes.config_count), int(sizes.n)
-    rwp = ((n + 31) // 32 + 3) // 4 * 4 if (n + 31) // 32 > 2 else (n + 31) // 32
+    rw = (n + 31) // 32
+    rwp = rw if rw <= 2 else (rw + 3) // 4 * 4
     slots = int(st.slots)
-    # algorithmic bytes of one cop-turn launch: read every config's marked row and its input
-    # frontier row (all value slots) once, read+write the frontier flags, write the new marks
-    cop_marks = sum(solver.pass_counts) / 2.0 / max(cop_launches, 1)
-    alg_bytes = C * (4 * rwp * (1 + slots) + 2) + cop_marks * (1 + 4.0 / 32)
-    achieved = alg_bytes / (mean_ms / 1e3) / 1e9
+    k_ms = float(st.init_ms)
+    # algorithmic bytes of one k_init_pass1 launch: every table byte written once (S), both
+    # marked bit planes written (2 * C * rwp * 4), column 1's frontier rows written
+    # (C * slots * rwp * 4) and both flag planes (2 * C)
+    k_bytes = S + 2 * C * rwp * 4 + C * slots * rwp * 4 + 2 * C
+    achieved = k_bytes / (k_ms / 1e3) / 1e9 if k_ms > 0 else None
     peak, peak_kind = measured_peak_hbm()
     traffic = traffic_per_launch()
+    # whole-solve algorithmic bytes (the state store's minimal traffic): per level both
+    # resolved bit planes read (S/8), the frontier plane read and the next written (S/16 each),
+    # the resolved bits written (S/8) = 3S/8; 2 B of capture depth per resolved state; 1 B of
+    # escape counter per state written and read once (S)
+    resolved = 2 * int(solver.base_captures) + sum(solver.pass_counts)
+    solve_bytes = passes * 3 * S / 8 + 2 * resolved + S
+    solve_achieved = solve_bytes / (ms / args.steps / 1e3) / 1e9
     solver.close()
 
     # e2e: the public one-call API from pinned host CSR to the pinned host table
@@ -366,6 +400,7 @@ def run_gpu(args) -> None:
     if rank == 0 and not args.headline_only:
         extra["batched"] = batched_workload(ctx)
         extra["limited_visibility"] = limited_visibility_workload(ctx)
+        extra["serving"] = serving_workload(args.serving_requests, args.serving_rate)
     if rank == 0:
         base = cpu_baseline(g, k, p, passes) if not args.no_cpu_baseline else None
         line = {
@@ -379,9 +414,12 @@ def run_gpu(args) -> None:
                     "h2d_bytes_per_step": int(row_ptr.nbytes + col.nbytes),
                     "d2h_bytes_per_step": int(S + 8 * len(counts) + ctypes.sizeof(vv))},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic, "kernel": "k_cop (cop turn)",
-                         "peak_source": peak_kind, "launches": cop_launches, "mean_launch_ms": mean_ms,
-                         "alg_bytes_per_launch": alg_bytes},
+                         "frac": achieved / peak if achieved else None, "traffic": traffic,
+                         "kernel": "k_init_pass1 (initializeCaptures + pass 1, one launch per solve)",
+                         "peak_source": peak_kind, "mean_launch_ms": k_ms, "alg_bytes_per_launch": k_bytes,
+                         "solve": {"alg_bytes": solve_bytes, "achieved": solve_achieved,
+                                   "frac": solve_achieved / peak, "levels": passes,
+                                   "resolved_states": resolved}},
             "cpu_baseline": base,
             "clocks": clocks.summary(),
             "gpu_launches": launches_per_step * args.steps,
@@ -401,7 +439,9 @@ def main() -> None:
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--headline-only", action="store_true",
-                    help="skip the batched and limited-visibility workloads")
+                    help="skip the batched, limited-visibility and serving workloads")
+    ap.add_argument("--serving-requests", type=int, default=2000)
+    ap.add_argument("--serving-rate", type=float, default=60.0, help="requests per second")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

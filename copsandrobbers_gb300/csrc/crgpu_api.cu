@@ -20,6 +20,7 @@ void launch_cop(const V1Dev& d, int col, int nx, int direct, int grid, cudaStrea
 void launch_and(const V1Dev& d, int col, bool p1, int grid, cudaStream_t st);
 void launch_prep(const V1Dev& d, int col, int nx, int grid, cudaStream_t st);
 void launch_init(const V1Dev& d, int grid, cudaStream_t st);
+void launch_init_pass1(const V1Dev& d, int grid, cudaStream_t st);
 void launch_verdict(const V1Dev& d, int cols, unsigned long long* best, int grid, cudaStream_t st);
 void launch_popcount(const uint32_t* plane, size_t words, unsigned long long* out, int grid,
                      cudaStream_t st);
@@ -66,6 +67,8 @@ struct cr_solver {
     uint32_t* d_nbr = nullptr;
     uint32_t* d_iso = nullptr;
     uint32_t* d_rhop = nullptr;
+    uint8_t* d_cover = nullptr;   // first-pass neighbour-slot masks (p = 1, max degree <= 32)
+    int cover_w = 0, npad = 0;
     ColMeta* d_meta = nullptr;
     unsigned long long* d_counters = nullptr;  // [0] pass_new, [1] verdict key, [2] scratch
     unsigned int* d_err = nullptr;
@@ -78,6 +81,10 @@ struct cr_solver {
     // phase state
     bool initialized = false;
     bool finished = false;
+    // p = 1: initializeCaptures is folded into the first pass (one sweep writes the table);
+    // set between cr_solver_init and that pass, and undone by materialize_init() when the
+    // post-initializeCaptures state is read first
+    bool init_pending = false;
     uint64_t base_caps = 0;
     std::vector<uint64_t> pass_counts;
     cr_solve_stats stats{};
@@ -217,6 +224,7 @@ uint64_t cr_solver_footprint(int32_t n, int32_t k, int32_t p, int32_t rules) {
     b += (uint64_t)cols * C;                             // flags
     b += C * (uint64_t)k * 2;                            // configs
     b += (uint64_t)n * rwp * 4 * 3 + (uint64_t)k * (n + 1) * 4 + (1u << 16);
+    if (cols == 2) b += (2ull * n + 1) * (uint64_t)((n + 7) & ~7) * 4;   // first-pass cover masks
     return b;
 }
 
@@ -225,7 +233,7 @@ static void free_v1(cr_solver* s) {
     s->pass_graph = nullptr;
     void* ptrs[] = {s->d_rp, s->d_col, s->d_binom, s->d_configs, s->d_hop, s->d_table,
                     s->d_marked, s->d_front, s->d_fflag, s->d_meta, s->d_counters, s->d_err,
-                    s->d_heads, s->d_trans, s->d_cand, s->d_cflag, s->d_rrp, s->d_rcol, s->d_nbr, s->d_iso, s->d_rhop};
+                    s->d_heads, s->d_trans, s->d_cand, s->d_cflag, s->d_rrp, s->d_rcol, s->d_nbr, s->d_iso, s->d_rhop, s->d_cover};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     s->d_rp = nullptr; s->d_col = nullptr; s->d_binom = nullptr; s->d_configs = nullptr;
@@ -233,6 +241,7 @@ static void free_v1(cr_solver* s) {
     s->d_fflag = nullptr; s->d_meta = nullptr; s->d_counters = nullptr; s->d_err = nullptr;
     s->d_heads = nullptr; s->d_trans = nullptr; s->d_cand = nullptr; s->d_cflag = nullptr;
     s->d_rrp = nullptr; s->d_rcol = nullptr; s->d_nbr = nullptr; s->d_iso = nullptr; s->d_rhop = nullptr;
+    s->d_cover = nullptr;
     if (s->h_pinned) cudaFreeHost(s->h_pinned);
     s->h_pinned = nullptr;
     cudaEvent_t evs[] = {s->ev0, s->ev1, s->evc0, s->evc1};
@@ -254,6 +263,9 @@ static V1Dev dev_view(const cr_solver* s) {
     d.g.isolated = s->d_iso;
     d.g.rhop = s->d_rhop;
     d.g.maxdeg = s->maxdeg;
+    d.g.cover = s->d_cover;
+    d.g.cover_w = s->cover_w;
+    d.g.npad = s->npad;
     d.k = s->k;
     d.cols = s->cols;
     d.S = s->S;
@@ -340,6 +352,34 @@ static int alloc_v1(cr_solver* s) {
     CR_CUDA(ctx, cudaMemcpyAsync(s->d_nbr, nbr.data(), nbr.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
     CR_CUDA(ctx, cudaMemcpyAsync(s->d_rrp, rrp.data(), rrp.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
     CR_CUDA(ctx, cudaMemcpyAsync(s->d_rcol, rcol.data(), rcol.size() * 2, cudaMemcpyHostToDevice, ctx->stream));
+    // neighbour-slot masks of the folded first pass (two columns, out-degrees <= 32):
+    // plane 0 [c][r] slots of r in {c} + N(c), plane 1 [c][r] slots of r equal to c,
+    // plane 2 [r] every slot of r; masks of cover_w bytes, rows padded to npad robbers
+    s->cover_w = 0;
+    if (s->cols == 2 && s->maxdeg <= 32) {
+        const int W = s->maxdeg <= 8 ? 1 : (s->maxdeg <= 16 ? 2 : 4);
+        const int n = s->n, npad = (n + 7) & ~7;
+        const size_t plane = (size_t)n * npad;
+        std::vector<uint32_t> m(2 * plane + npad, 0);
+        for (int r = 0; r < n; ++r) {
+            const uint32_t e0 = s->h_rp[r], deg = s->h_rp[r + 1] - e0;
+            m[2 * plane + r] = deg == 32 ? 0xFFFFFFFFu : ((1u << deg) - 1u);
+            for (uint32_t j = 0; j < deg; ++j) {
+                const int v = s->h_col[e0 + j];
+                m[plane + (size_t)v * npad + r] |= 1u << j;      // slot j of r is the cop v
+                m[(size_t)v * npad + r] |= 1u << j;              // ... and so lies in N[v]
+                // slot j of r lies in N(c) for every c with v in N(c), i.e. c an in-neighbour of v
+                for (uint32_t f = rrp[v]; f < rrp[v + 1]; ++f) m[(size_t)rcol[f] * npad + r] |= 1u << j;
+            }
+        }
+        std::vector<uint8_t> bytes(m.size() * W);
+        for (size_t i = 0; i < m.size(); ++i)
+            for (int b = 0; b < W; ++b) bytes[i * W + b] = (uint8_t)(m[i] >> (8 * b));
+        CR_CUDA(ctx, cudaMalloc(&s->d_cover, bytes.size()));
+        CR_CUDA(ctx, cudaMemcpyAsync(s->d_cover, bytes.data(), bytes.size(), cudaMemcpyHostToDevice, ctx->stream));
+        s->cover_w = W;
+        s->npad = npad;
+    }
     CR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return CR_OK;
 }
@@ -490,6 +530,43 @@ static int v1_init(cr_solver* s, uint64_t* caps) {
     return CR_OK;
 }
 
+// initializeCaptures and pass 1 of a p = 1 solve in one kernel (init_pass1_body): every table
+// byte, both marked planes, column 1's frontier and both flag planes are written whole, so
+// nothing is cleared first.
+static int v1_init_pass1(cr_solver* s, uint64_t* found) {
+    cr_context* ctx = s->ctx;
+    cudaStream_t st = ctx->stream;
+    CR_CUDA(ctx, cudaMemsetAsync(s->d_counters, 0, 4 * sizeof(unsigned long long), st));
+    CR_CUDA(ctx, cudaMemsetAsync(s->d_err, 0, sizeof(unsigned), st));
+    ColMeta meta[2] = {ColMeta{0, 0, 0, 0, (int)std::min<uint64_t>(s->C, INT32_MAX), 0, {0, 0}},
+                       ColMeta{1, kEmptyLo, -1, 0, 0, 0, {0, 0}}};
+    CR_CUDA(ctx, cudaMemcpyAsync(s->d_meta, meta, sizeof(meta), cudaMemcpyHostToDevice, st));
+    V1Dev d = dev_view(s);
+    CR_CUDA(ctx, cudaEventRecord(s->evc0, st));
+    launch_init_pass1(d, s->grid_cop, st);
+    CR_CUDA(ctx, cudaGetLastError());
+    CR_CUDA(ctx, cudaEventRecord(s->evc1, st));
+    CR_CUDA(ctx, cudaMemcpyAsync(s->h_pinned, s->d_counters, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    CR_CUDA(ctx, cudaStreamSynchronize(st));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, s->evc0, s->evc1);
+    s->stats.init_ms = ms;
+    s->init_pending = false;
+    s->stats.kernel_launches += 1;
+    *found = s->h_pinned[0];
+    return CR_OK;
+}
+
+// The exact post-initializeCaptures state, for a caller that reads the table before pass 1.
+static int materialize_init(cr_solver* s) {
+    if (!s->init_pending) return CR_OK;
+    uint64_t caps = 0;
+    int rc = v1_init(s, &caps);
+    if (rc) return rc;
+    s->init_pending = false;
+    return CR_OK;
+}
+
 // Enqueue one pass: per column a prep kernel and its producer, then the pass counter copy.
 static int v1_enqueue_pass(cr_solver* s, bool profile) {
     cr_context* ctx = s->ctx;
@@ -555,7 +632,19 @@ int cr_solver_init(cr_solver* s, uint64_t* base_captures) {
     cr_context* ctx = s->ctx;
     CR_CUDA(ctx, cudaSetDevice(ctx->device));
     uint64_t caps = 0;
-    int rc = s->rules == CR_RULES_V1 ? v1_init(s, &caps) : crgpu::v2_init(s->v2, &caps, &s->stats, &ctx->err);
+    s->init_pending = false;
+    int rc = CR_OK;
+    if (s->rules == CR_RULES_V1 && s->cols == 2 && s->S >= 2 && s->cover_w > 0) {
+        // folded into pass 1; the capture count has a closed form: every configuration
+        // contributes its distinct cop vertices, and n * (multisets containing a given vertex)
+        // = n * (C(n+k-1, k) - C(n+k-2, k))
+        caps = (uint64_t)s->n * (binom_u64(s->n + s->k - 1, s->k) - binom_u64(s->n + s->k - 2, s->k));
+        s->init_pending = true;
+        s->stats.init_ms = 0;
+        s->stats.kernel_launches = 0;
+    } else {
+        rc = s->rules == CR_RULES_V1 ? v1_init(s, &caps) : crgpu::v2_init(s->v2, &caps, &s->stats, &ctx->err);
+    }
     if (rc) return rc;
     s->base_caps = caps;
     s->pass_counts.clear();
@@ -615,7 +704,7 @@ int cr_solver_pass(cr_solver* s, uint64_t* new_wins) {
     } else {
         for (int attempt = 0;; ++attempt) {
             CR_CUDA(ctx, cudaEventRecord(s->ev0, ctx->stream));
-            int rc = v1_pass(s, &f);
+            int rc = s->init_pending ? v1_init_pass1(s, &f) : v1_pass(s, &f);
             if (rc) return rc;
             CR_CUDA(ctx, cudaEventRecord(s->ev1, ctx->stream));
             CR_CUDA(ctx, cudaEventSynchronize(s->ev1));
@@ -658,6 +747,7 @@ int cr_solver_verdict(cr_solver* s, cr_verdict* out) {
     if (!s || !out) return CR_ERR_INVALID;
     cr_context* ctx = s->ctx;
     CR_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (int rc = materialize_init(s)) return rc;
     cudaStream_t st = ctx->stream;
     const unsigned long long init = ~0ull;
     CR_CUDA(ctx, cudaMemcpyAsync(s->d_counters + 1, &init, sizeof(init), cudaMemcpyHostToDevice, st));
@@ -717,6 +807,7 @@ int cr_solver_digest(cr_solver* s, uint64_t* digest) {
     if (!s || !digest) return CR_ERR_INVALID;
     cr_context* ctx = s->ctx;
     CR_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (int rc = materialize_init(s)) return rc;
     cudaStream_t st = ctx->stream;
     CR_CUDA(ctx, cudaMemsetAsync(s->d_counters + 2, 0, sizeof(unsigned long long), st));
     launch_digest(table_ptr(s), s->C * (size_t)s->n * s->cols, s->d_counters + 2, ctx->num_sms * 4, st);
@@ -729,6 +820,8 @@ int cr_solver_digest(cr_solver* s, uint64_t* digest) {
 
 int cr_solver_device_states(cr_solver* s, void** dev_ptr, size_t* bytes) {
     if (!s || !dev_ptr || !bytes) return CR_ERR_INVALID;
+    CR_CUDA(s->ctx, cudaSetDevice(s->ctx->device));
+    if (int rc = materialize_init(s)) return rc;
     *dev_ptr = (void*)table_ptr(s);
     *bytes = s->C * (size_t)s->n * s->cols;
     return CR_OK;
@@ -740,6 +833,7 @@ int cr_solver_read_states(cr_solver* s, uint8_t* dst, size_t bytes) {
     const size_t need = s->C * (size_t)s->n * s->cols;
     if (bytes < need) return fail(ctx, CR_ERR_INVALID, "states buffer holds %zu of %zu bytes", bytes, need);
     CR_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (int rc = materialize_init(s)) return rc;
     CR_CUDA(ctx, cudaMemcpyAsync(dst, table_ptr(s), need, cudaMemcpyDeviceToHost, ctx->stream));
     CR_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return CR_OK;

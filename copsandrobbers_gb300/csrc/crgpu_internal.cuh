@@ -53,6 +53,14 @@ struct DevGraph {
     const uint32_t* nbr;      // [n][rwp]: out-neighbour masks
     const uint32_t* isolated; // [rwp]: vertices without out-neighbours
     const uint32_t* rhop;     // [n][rwp]: bit r of row u set iff u is in hop(r) (transposed hop)
+    // Neighbour-slot masks for the first pass's closed form (cover_w bytes per mask, 0 = not
+    // built; npad = n rounded up to 8).  Bit j of a mask refers to r's j-th out-neighbour:
+    //   cover[c][r]            bit j set iff that neighbour is c or an out-neighbour of c
+    //   cover[n + c][r]        bit j set iff that neighbour is c
+    //   cover[2n][r]           every slot of r (deg(r) low bits)
+    const uint8_t* cover;
+    int cover_w;
+    int npad;
 };
 
 // Everything one v1 solve's kernels touch.

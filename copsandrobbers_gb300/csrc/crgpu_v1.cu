@@ -45,6 +45,8 @@ using namespace grid;
 
 __global__ void k_prep(V1Dev d, int col, int nx) { prep_body(d, col, nx, blockIdx.x, gridDim.x); }
 __global__ void k_init(V1Dev d, int K) { init_body(d, K, blockIdx.x, gridDim.x); }
+template <int K, int W>
+__global__ void __launch_bounds__(256) k_init_pass1(V1Dev d) { init_pass1_body<K, W>(d, blockIdx.x, gridDim.x); }
 
 template <int K, int NWP, int G>
 __global__ void __launch_bounds__(256) k_cop_pull(V1Dev d, int col, int nx) {
@@ -191,6 +193,24 @@ void launch_prep(const V1Dev& d, int col, int nx, int grid, cudaStream_t st) {
 }
 
 void launch_init(const V1Dev& d, int grid, cudaStream_t st) { k_init<<<grid, 256, 0, st>>>(d, d.k); }
+
+template <int W>
+static void launch_init_pass1_w(const V1Dev& d, int grid, size_t sm, cudaStream_t st) {
+    switch (d.k) {
+        case 1: k_init_pass1<1, W><<<grid, 256, sm, st>>>(d); break;
+        case 2: k_init_pass1<2, W><<<grid, 256, sm, st>>>(d); break;
+        case 3: k_init_pass1<3, W><<<grid, 256, sm, st>>>(d); break;
+        default: k_init_pass1<4, W><<<grid, 256, sm, st>>>(d); break;
+    }
+}
+
+// Requires d.g.cover (cover_w 1, 2 or 4) and two columns.
+void launch_init_pass1(const V1Dev& d, int grid, cudaStream_t st) {
+    const size_t sm = (size_t)(256 / 32) * pass1_warp_words(d.g.rwp) * 4;
+    if (d.g.cover_w == 1) launch_init_pass1_w<1>(d, grid, sm, st);
+    else if (d.g.cover_w == 2) launch_init_pass1_w<2>(d, grid, sm, st);
+    else launch_init_pass1_w<4>(d, grid, sm, st);
+}
 
 void launch_verdict(const V1Dev& d, int cols, unsigned long long* best, int grid, cudaStream_t st) {
     k_verdict<<<grid, 256, 0, st>>>(d.table, d.marked, d.C, d.g.n, d.g.rw, d.g.rwp, cols, best);

@@ -153,6 +153,272 @@ __device__ CR_BODY_INLINE void init_body(const V1Dev& d, int K, unsigned wk, uns
     if ((threadIdx.x & 31) == 0 && caps) atomicAdd(d.pass_new, (unsigned long long)caps);
 }
 
+// Shared-memory words per warp of init_pass1_body.
+__host__ __device__ inline int pass1_warp_words(int rwp) { return 4 * rwp; }
+
+// 4 bits -> 4 bytes of 0xFF / 0x00 (bit i -> byte i).
+__device__ __forceinline__ uint32_t nibble_bytes(uint32_t b) {
+    return ((b * 0x00204081u) & 0x01010101u) * 0xFFu;
+}
+
+// Cover masks of 8 consecutive robbers (cover_w = W bytes each), packed in 2W words.
+template <int W>
+struct Cov8 {
+    static constexpr int NW = 2 * W;
+    uint32_t w[NW];
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int q = 0; q < NW; ++q) w[q] = 0u;
+    }
+    __device__ __forceinline__ void load(const uint8_t* p) {   // p is 8W-byte aligned
+        if (W == 1) {
+            const uint2 v = CR_LDG(reinterpret_cast<const uint2*>(p));
+            w[0] = v.x; w[1] = v.y;
+        } else {
+#pragma unroll
+            for (int h = 0; h < W / 2; ++h) {
+                const uint4 v = CR_LDG(reinterpret_cast<const uint4*>(p) + h);
+                w[4 * h] = v.x; w[4 * h + 1] = v.y; w[4 * h + 2] = v.z; w[4 * h + 3] = v.w;
+            }
+        }
+    }
+    __device__ __forceinline__ void orr(const Cov8& o) {
+#pragma unroll
+        for (int q = 0; q < NW; ++q) w[q] |= o.w[q];
+    }
+    // bit j set iff robber j's mask equals o's
+    __device__ __forceinline__ uint32_t eq_bits(const Cov8& o) const {
+        uint32_t b = 0;
+        if (W == 1) {
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const uint32_t m = __vcmpeq4(w[q], o.w[q]);
+                b |= (((((m >> 7) & 0x01010101u) * 0x01020408u) >> 24) & 0xFu) << (4 * q);
+            }
+        } else if (W == 2) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const uint32_t m = __vcmpeq2(w[q], o.w[q]);
+                b |= (((m >> 15) & 1u) | ((m >> 30) & 2u)) << (2 * q);
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < 8; ++q) b |= (uint32_t)(w[q] == o.w[q]) << q;
+        }
+        return b;
+    }
+};
+
+// The next sorted multiset in lexicographic order (the configuration order).
+template <int K>
+__device__ __forceinline__ void next_multiset(int (&c)[K], int n) {
+    int i = 0;   // the rightmost position below n - 1 (registers only: no indexed access)
+#pragma unroll
+    for (int j = 1; j < K; ++j)
+        if (c[j] < n - 1) i = j;
+    int v = 0;
+#pragma unroll
+    for (int j = 0; j < K; ++j)
+        if (j == i) v = c[j] + 1;
+#pragma unroll
+    for (int j = 0; j < K; ++j)
+        if (j >= i) c[j] = v;
+}
+
+// initializeCaptures and the whole first pass of a p = 1 solve (two columns) in one sweep that
+// writes every table byte once.  After initializeCaptures only the captures are marked (round
+// 0, both columns), so the first pass has closed forms:
+//   column 0 (cops to move, k_cops_visibility.cpp:160-197): a robber on N(cops) is caught by
+//          one cop move when every cop can move -- round 1;
+//   column 1 (robber to move, :235-288): a robber r off the cops is lost when every move lands
+//          on a column-0 mark, N(r) within M0 = cops | N(cops) (cops alone when some cop cannot
+//          move); its round is 1 + the largest column-0 round among N(r): 2 when some
+//          neighbour is not a cop, else 1.
+// With the cover masks both tests are ORs over the k cops: N(r) lies in M0 iff the OR of
+// cover[c][r] is every slot of r, and N(r) lies in the cops iff the OR of cover[n + c][r] is.
+// Column 1's marks form its output frontier (value base 1: slot 0 holds round 1, slot 1
+// round 2).  Column 0's frontier is read only through its flags and range, and every
+// configuration has captures, so every column-0 flag is set.
+// Each warp sweeps a contiguous range of configurations, stepping the multiset itself, and
+// keeps the masks of all cops but the last (they change once per n - c[k-2] steps); lane l
+// owns robbers 8l .. 8l+7 of each 256-vertex block, i.e. one 16-byte piece of the row.
+// The caller sets meta[0] = {0, 0, 0, 0, C, 0}, meta[1] = {1, empty, -1, 0, 0, 0} and zeroes
+// the pass counter; the pass counter then holds the first pass's count.
+template <int K, int W>
+__device__ CR_BODY_INLINE void init_pass1_body(const V1Dev& d, unsigned wk, unsigned nwk) {
+    extern __shared__ uint32_t sm[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n = d.g.n, rw = d.g.rw, rwp = d.g.rwp, S = d.S, npad = d.g.npad;
+    uint32_t* wcap = sm + warp * pass1_warp_words(rwp);  // the cops
+    uint32_t* wseed = wcap + rwp;                        // N(cops) \ cops (round 1)
+    uint8_t* wa1 = reinterpret_cast<uint8_t*>(wseed + rwp);      // column-1 marks, round 1
+    uint8_t* wa2 = reinterpret_cast<uint8_t*>(wseed + 2 * rwp);  // column-1 marks, round 2
+    const uint32_t* CR_RESTRICT rp = d.g.row_ptr;
+    const uint8_t* CR_RESTRICT cover = d.g.cover;
+    const size_t plane = (size_t)n * npad * W;          // bytes of one cover plane
+    const bool aligned = (n & 7) == 0, single = n <= 256;
+    unsigned cnt = 0, rows1 = 0, any_seed = 0, any1 = 0, any2 = 0;
+    const size_t nwarps = (size_t)nwk * (blockDim.x >> 5);
+    const size_t chunk = (d.C + nwarps - 1) / nwarps;
+    const size_t cb = ((size_t)wk * (blockDim.x >> 5) + warp) * chunk;
+    const size_t ce = cb + chunk < d.C ? cb + chunk : d.C;
+    int c[K];
+    if (cb < ce) {
+#pragma unroll
+        for (int i = 0; i < K; ++i) c[i] = CR_LDG(&d.configs[cb * K + i]);
+    }
+    // masks of the cops c[0 .. K-2], valid while they stay put (single-block rows only)
+    int pre[K > 1 ? K - 1 : 1];
+#pragma unroll
+    for (int i = 0; i < K - 1; ++i) pre[i] = -1;
+    Cov8<W> xpre, epre, f;
+    bool mpre = true;
+    uint32_t npre = 0;
+    xpre.zero();
+    epre.zero();
+    if (single && lane * 8 < n) f.load(cover + 2 * plane + (size_t)lane * 8 * W);
+    for (size_t cid = cb; cid < ce; ++cid) {
+        if (cid > cb) next_multiset<K>(c, n);
+        const int cl = c[K - 1];
+        bool same = true;
+#pragma unroll
+        for (int i = 0; i < K - 1; ++i) same &= pre[i] == c[i];
+        if (!same) {
+            // the leading cops moved: rebuild their masks
+            xpre.zero();
+            epre.zero();
+            mpre = true;
+            npre = 0;
+#pragma unroll
+            for (int i = 0; i < K - 1; ++i) {
+                pre[i] = c[i];
+                mpre &= CR_LDG(&rp[c[i] + 1]) > CR_LDG(&rp[c[i]]);
+                if (lane < rwp) npre |= CR_LDG(&d.g.nbr[(size_t)c[i] * rwp + lane]);
+                if (single && lane * 8 < n) {
+                    Cov8<W> t;
+                    t.load(cover + ((size_t)c[i] * npad + lane * 8) * W);
+                    xpre.orr(t);
+                    t.load(cover + plane + ((size_t)c[i] * npad + lane * 8) * W);
+                    epre.orr(t);
+                }
+            }
+        }
+        const bool moves = mpre && CR_LDG(&rp[cl + 1]) > CR_LDG(&rp[cl]);
+        if (lane < rwp) {
+            uint32_t caps = 0;
+#pragma unroll
+            for (int i = 0; i < K; ++i)
+                if ((c[i] >> 5) == lane) caps |= 1u << (c[i] & 31);
+            const uint32_t x = moves ? (npre | CR_LDG(&d.g.nbr[(size_t)cl * rwp + lane])) : 0u;
+            wcap[lane] = caps;
+            wseed[lane] = x & ~caps;
+            reinterpret_cast<uint32_t*>(wa1)[lane] = 0u;   // bytes past n stay zero
+            reinterpret_cast<uint32_t*>(wa2)[lane] = 0u;
+            d.marked[cid * rwp + lane] = caps | x;
+            cnt += __popc(x & ~caps);
+            any_seed |= x & ~caps;
+        }
+        __syncwarp();
+        for (int r0 = lane * 8; r0 < n; r0 += 256) {
+            const uint32_t capb = (wcap[r0 >> 5] >> (r0 & 31)) & 0xFFu;
+            const uint32_t seedb = (wseed[r0 >> 5] >> (r0 & 31)) & 0xFFu;
+            const uint32_t validb = n - r0 >= 8 ? 0xFFu : ((1u << (n - r0)) - 1u);
+            // every slot of r in M0 (comp) / some slot of r not a cop (deep)
+            Cov8<W> x, e, t;
+            if (single) {
+                x = xpre;
+                e = epre;
+            } else {
+                f.load(cover + 2 * plane + (size_t)r0 * W);
+                x.zero();
+                e.zero();
+#pragma unroll
+                for (int i = 0; i < K - 1; ++i) {
+                    t.load(cover + ((size_t)c[i] * npad + r0) * W);
+                    x.orr(t);
+                    t.load(cover + plane + ((size_t)c[i] * npad + r0) * W);
+                    e.orr(t);
+                }
+            }
+            t.load(cover + plane + ((size_t)cl * npad + r0) * W);
+            e.orr(t);
+            if (moves) {
+                t.load(cover + ((size_t)cl * npad + r0) * W);
+                x.orr(t);
+            } else {
+                x = e;
+            }
+            const uint32_t compb = x.eq_bits(f);
+            const uint32_t deepb = ~e.eq_bits(f) & 0xFFu;
+            const uint32_t a = compb & ~capb & validb;
+            const uint32_t a2 = a & deepb, a1 = a & ~deepb;
+            // bytes: column 0 = 0x01 cop / 0x03 seed / 0xFE; column 1 = 0x01 cop / 0x03 round 1
+            // / 0x05 round 2 / 0xFE; state (r, col) is byte 2r + col of the row
+            uint32_t q[4];
+#pragma unroll
+            for (int g = 0; g < 2; ++g) {
+                const uint32_t mc = nibble_bytes((capb >> (4 * g)) & 0xFu);
+                const uint32_t ms = nibble_bytes((seedb >> (4 * g)) & 0xFu);
+                const uint32_t m1 = nibble_bytes((a1 >> (4 * g)) & 0xFu);
+                const uint32_t m2 = nibble_bytes((a2 >> (4 * g)) & 0xFu);
+                const uint32_t c0 = (mc & 0x01010101u) | (ms & 0x03030303u) | (~(mc | ms) & 0xFEFEFEFEu);
+                const uint32_t c1 = (mc & 0x01010101u) | (m1 & 0x03030303u) | (m2 & 0x05050505u) |
+                                    (~(mc | m1 | m2) & 0xFEFEFEFEu);
+                q[2 * g] = __byte_perm(c0, c1, 0x5140);
+                q[2 * g + 1] = __byte_perm(c0, c1, 0x7362);
+            }
+            uint8_t* dst = d.table + (cid * n + r0) * 2;
+            if (aligned) {
+                *reinterpret_cast<uint4*>(dst) = make_uint4(q[0], q[1], q[2], q[3]);
+            } else {
+                for (int b = 0; b < 16 && r0 + (b >> 1) < n; ++b) dst[b] = (uint8_t)(q[b >> 2] >> ((b & 3) * 8));
+            }
+            wa1[r0 >> 3] = (uint8_t)a1;
+            wa2[r0 >> 3] = (uint8_t)a2;
+            cnt += __popc(a1) + __popc(a2);
+            any1 |= a1;
+            any2 |= a2;
+        }
+        __syncwarp();
+        // column 1: marked row, frontier row (slot 0 = round 1, slot 1 = round 2), flag
+        uint32_t new1 = 0;
+        if (lane < rwp) {
+            const uint32_t w1 = lane < rw ? reinterpret_cast<const uint32_t*>(wa1)[lane] : 0u;
+            const uint32_t w2 = lane < rw ? reinterpret_cast<const uint32_t*>(wa2)[lane] : 0u;
+            new1 = w1 | w2;
+            d.marked[((size_t)d.C + cid) * rwp + lane] = wcap[lane] | new1;
+        }
+        const bool changed = __any_sync(FULL_MASK, new1 != 0u);
+        uint32_t* frow = d.front + ((size_t)d.C + cid) * S * rwp;
+        for (int e = lane; e < S * rwp; e += 32) {
+            const int s = e / rwp, w = e - s * rwp;
+            uint32_t val = 0u;
+            if (s < 2 && w < rw) val = reinterpret_cast<const uint32_t*>(s == 0 ? wa1 : wa2)[w];
+            frow[e] = val;
+        }
+        if (lane == 0) {
+            d.fflag[cid] = 1;
+            d.fflag[(size_t)d.C + cid] = changed ? 1 : 0;
+            rows1 += changed ? 1u : 0u;
+        }
+        __syncwarp();
+    }
+    cnt = __reduce_add_sync(FULL_MASK, cnt);
+    rows1 = __reduce_add_sync(FULL_MASK, rows1);
+    any_seed = __reduce_or_sync(FULL_MASK, any_seed);
+    any1 = __reduce_or_sync(FULL_MASK, any1);
+    any2 = __reduce_or_sync(FULL_MASK, any2);
+    if (lane == 0) {
+        if (cnt) atomicAdd(d.pass_new, (unsigned long long)cnt);
+        if (rows1) atomicAdd(&d.meta[1].rows, (int)rows1);
+        if (any_seed) atomicMax(&d.meta[0].hi, 1);
+        if (any1 | any2) {
+            atomicMin(&d.meta[1].lo, any1 ? 1 : 2);
+            atomicMax(&d.meta[1].hi, any2 ? 2 : 1);
+        }
+    }
+}
+
 // ---- lane groups ---------------------------------------------------------------------
 // A warp works on CPW = 32 / G configurations at once, G lanes per configuration (G >= rwp,
 // so every word of a robber row has its own lane).  All lanes of a warp run the same control

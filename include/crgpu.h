@@ -78,7 +78,8 @@ typedef struct cr_table_sizes {
 
 /* Timing and traffic of the last solve, device-side (CUDA events on the solver's stream). */
 typedef struct cr_solve_stats {
-    double init_ms;            /* initializeCaptures */
+    double init_ms;            /* initializeCaptures; for p = 1 v1 solves, where it is folded
+                                  into pass 1, the time of that one kernel */
     double main_ms;            /* mainLoop to the fixed point */
     double cop_step_ms;        /* sum over cop-turn kernel launches (when profiling) */
     int64_t cop_step_launches;

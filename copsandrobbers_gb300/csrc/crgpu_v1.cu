@@ -206,7 +206,7 @@ static void launch_init_pass1_w(const V1Dev& d, int grid, size_t sm, cudaStream_
 
 // Requires d.g.cover (cover_w 1, 2 or 4) and two columns.
 void launch_init_pass1(const V1Dev& d, int grid, cudaStream_t st) {
-    const size_t sm = (size_t)(256 / 32) * pass1_warp_words(d.g.rwp) * 4;
+    const size_t sm = 0;
     if (d.g.cover_w == 1) launch_init_pass1_w<1>(d, grid, sm, st);
     else if (d.g.cover_w == 2) launch_init_pass1_w<2>(d, grid, sm, st);
     else launch_init_pass1_w<4>(d, grid, sm, st);

@@ -153,12 +153,13 @@ __device__ CR_BODY_INLINE void init_body(const V1Dev& d, int K, unsigned wk, uns
     if ((threadIdx.x & 31) == 0 && caps) atomicAdd(d.pass_new, (unsigned long long)caps);
 }
 
-// Shared-memory words per warp of init_pass1_body.
-__host__ __device__ inline int pass1_warp_words(int rwp) { return 4 * rwp; }
-
 // 4 bits -> 4 bytes of 0xFF / 0x00 (bit i -> byte i).
 __device__ __forceinline__ uint32_t nibble_bytes(uint32_t b) {
     return ((b * 0x00204081u) & 0x01010101u) * 0xFFu;
+}
+// The top bit of each byte -> 4 bits (byte i -> bit i).
+__device__ __forceinline__ uint32_t byte_bits(uint32_t m) {
+    return ((((m >> 7) & 0x01010101u) * 0x01020408u) >> 24) & 0xFu;
 }
 
 // Cover masks of 8 consecutive robbers (cover_w = W bytes each), packed in 2W words.
@@ -225,6 +226,15 @@ __device__ __forceinline__ void next_multiset(int (&c)[K], int n) {
         if (j >= i) c[j] = v;
 }
 
+// Byte-wise tests on 4 packed bytes, exact (no carries between bytes): the top bit of byte i
+// is set iff byte i of z is zero / non-zero.
+__device__ __forceinline__ uint32_t zero_bytes_hi(uint32_t z) {
+    return ~(((z & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | z) & 0x80808080u;
+}
+__device__ __forceinline__ uint32_t nonzero_bytes_hi(uint32_t z) {
+    return (((z & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | z) & 0x80808080u;
+}
+
 // initializeCaptures and the whole first pass of a p = 1 solve (two columns) in one sweep that
 // writes every table byte once.  After initializeCaptures only the captures are marked (round
 // 0, both columns), so the first pass has closed forms:
@@ -240,23 +250,21 @@ __device__ __forceinline__ void next_multiset(int (&c)[K], int n) {
 // round 2).  Column 0's frontier is read only through its flags and range, and every
 // configuration has captures, so every column-0 flag is set.
 // Each warp sweeps a contiguous range of configurations, stepping the multiset itself, and
-// keeps the masks of all cops but the last (they change once per n - c[k-2] steps); lane l
-// owns robbers 8l .. 8l+7 of each 256-vertex block, i.e. one 16-byte piece of the row.
+// keeps the masks of all cops but the last (they change once per n - c[k-2] steps).  Lane l
+// owns robbers 8l .. 8l+7 of each 256-vertex block, i.e. one 16-byte piece of the row, and
+// the 8-bit pieces of the marked and frontier rows, which four lanes assemble into a word.
 // The caller sets meta[0] = {0, 0, 0, 0, C, 0}, meta[1] = {1, empty, -1, 0, 0, 0} and zeroes
 // the pass counter; the pass counter then holds the first pass's count.
 template <int K, int W>
 __device__ CR_BODY_INLINE void init_pass1_body(const V1Dev& d, unsigned wk, unsigned nwk) {
-    extern __shared__ uint32_t sm[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int n = d.g.n, rw = d.g.rw, rwp = d.g.rwp, S = d.S, npad = d.g.npad;
-    uint32_t* wcap = sm + warp * pass1_warp_words(rwp);  // the cops
-    uint32_t* wseed = wcap + rwp;                        // N(cops) \ cops (round 1)
-    uint8_t* wa1 = reinterpret_cast<uint8_t*>(wseed + rwp);      // column-1 marks, round 1
-    uint8_t* wa2 = reinterpret_cast<uint8_t*>(wseed + 2 * rwp);  // column-1 marks, round 2
     const uint32_t* CR_RESTRICT rp = d.g.row_ptr;
+    const uint32_t* CR_RESTRICT nbr = d.g.nbr;
     const uint8_t* CR_RESTRICT cover = d.g.cover;
     const size_t plane = (size_t)n * npad * W;          // bytes of one cover plane
     const bool aligned = (n & 7) == 0, single = n <= 256;
+    const bool padded = rw != rwp || S > 2;             // row words beyond the marks to clear
     unsigned cnt = 0, rows1 = 0, any_seed = 0, any1 = 0, any2 = 0;
     const size_t nwarps = (size_t)nwk * (blockDim.x >> 5);
     const size_t chunk = (d.C + nwarps - 1) / nwarps;
@@ -267,17 +275,26 @@ __device__ CR_BODY_INLINE void init_pass1_body(const V1Dev& d, unsigned wk, unsi
 #pragma unroll
         for (int i = 0; i < K; ++i) c[i] = CR_LDG(&d.configs[cb * K + i]);
     }
-    // masks of the cops c[0 .. K-2], valid while they stay put (single-block rows only)
+    // state of the cops c[0 .. K-2], kept while they stay put (single-block rows only)
     int pre[K > 1 ? K - 1 : 1];
 #pragma unroll
     for (int i = 0; i < K - 1; ++i) pre[i] = -1;
     Cov8<W> xpre, epre, f;
     bool mpre = true;
-    uint32_t npre = 0;
+    uint32_t npre = 0;                                   // their out-neighbours, word lane/4
     xpre.zero();
     epre.zero();
     if (single && lane * 8 < n) f.load(cover + 2 * plane + (size_t)lane * 8 * W);
-    for (size_t cid = cb; cid < ce; ++cid) {
+    // row pointers advanced per configuration (no per-row index arithmetic)
+    uint8_t* trow = d.table + cb * n * 2;
+    uint32_t* m0row = d.marked + cb * rwp;
+    uint32_t* m1row = d.marked + ((size_t)d.C + cb) * rwp;
+    const int frow_words = S * rwp;
+    uint32_t* frow = d.front + ((size_t)d.C + cb) * frow_words;
+    uint8_t* fl0 = d.fflag + cb;
+    uint8_t* fl1 = d.fflag + (size_t)d.C + cb;
+    for (size_t cid = cb; cid < ce; ++cid, trow += 2 * n, m0row += rwp, m1row += rwp, frow += frow_words,
+                ++fl0, ++fl1) {
         if (cid > cb) next_multiset<K>(c, n);
         const int cl = c[K - 1];
         bool same = true;
@@ -293,115 +310,144 @@ __device__ CR_BODY_INLINE void init_pass1_body(const V1Dev& d, unsigned wk, unsi
             for (int i = 0; i < K - 1; ++i) {
                 pre[i] = c[i];
                 mpre &= CR_LDG(&rp[c[i] + 1]) > CR_LDG(&rp[c[i]]);
-                if (lane < rwp) npre |= CR_LDG(&d.g.nbr[(size_t)c[i] * rwp + lane]);
                 if (single && lane * 8 < n) {
+                    npre |= CR_LDG(&nbr[c[i] * rwp + (lane >> 2)]);
                     Cov8<W> t;
-                    t.load(cover + ((size_t)c[i] * npad + lane * 8) * W);
+                    t.load(cover + (uint32_t)(c[i] * npad + lane * 8) * W);
                     xpre.orr(t);
-                    t.load(cover + plane + ((size_t)c[i] * npad + lane * 8) * W);
+                    t.load(cover + plane + (uint32_t)(c[i] * npad + lane * 8) * W);
                     epre.orr(t);
                 }
             }
         }
         const bool moves = mpre && CR_LDG(&rp[cl + 1]) > CR_LDG(&rp[cl]);
-        if (lane < rwp) {
-            uint32_t caps = 0;
+        bool changed = false;
+        for (int r0 = lane * 8, it = 0; it * 256 < n; r0 += 256, ++it) {
+            uint32_t capb = 0, seedb = 0, a1 = 0, a2 = 0;
+            if (r0 < n) {
 #pragma unroll
-            for (int i = 0; i < K; ++i)
-                if ((c[i] >> 5) == lane) caps |= 1u << (c[i] & 31);
-            const uint32_t x = moves ? (npre | CR_LDG(&d.g.nbr[(size_t)cl * rwp + lane])) : 0u;
-            wcap[lane] = caps;
-            wseed[lane] = x & ~caps;
-            reinterpret_cast<uint32_t*>(wa1)[lane] = 0u;   // bytes past n stay zero
-            reinterpret_cast<uint32_t*>(wa2)[lane] = 0u;
-            d.marked[cid * rwp + lane] = caps | x;
-            cnt += __popc(x & ~caps);
-            any_seed |= x & ~caps;
-        }
-        __syncwarp();
-        for (int r0 = lane * 8; r0 < n; r0 += 256) {
-            const uint32_t capb = (wcap[r0 >> 5] >> (r0 & 31)) & 0xFFu;
-            const uint32_t seedb = (wseed[r0 >> 5] >> (r0 & 31)) & 0xFFu;
-            const uint32_t validb = n - r0 >= 8 ? 0xFFu : ((1u << (n - r0)) - 1u);
-            // every slot of r in M0 (comp) / some slot of r not a cop (deep)
-            Cov8<W> x, e, t;
-            if (single) {
-                x = xpre;
-                e = epre;
-            } else {
-                f.load(cover + 2 * plane + (size_t)r0 * W);
-                x.zero();
-                e.zero();
-#pragma unroll
-                for (int i = 0; i < K - 1; ++i) {
-                    t.load(cover + ((size_t)c[i] * npad + r0) * W);
-                    x.orr(t);
-                    t.load(cover + plane + ((size_t)c[i] * npad + r0) * W);
-                    e.orr(t);
+                for (int i = 0; i < K; ++i) {
+                    const unsigned dv = (unsigned)(c[i] - r0);
+                    if (dv < 8u) capb |= 1u << dv;
                 }
-            }
-            t.load(cover + plane + ((size_t)cl * npad + r0) * W);
-            e.orr(t);
-            if (moves) {
-                t.load(cover + ((size_t)cl * npad + r0) * W);
-                x.orr(t);
-            } else {
-                x = e;
-            }
-            const uint32_t compb = x.eq_bits(f);
-            const uint32_t deepb = ~e.eq_bits(f) & 0xFFu;
-            const uint32_t a = compb & ~capb & validb;
-            const uint32_t a2 = a & deepb, a1 = a & ~deepb;
-            // bytes: column 0 = 0x01 cop / 0x03 seed / 0xFE; column 1 = 0x01 cop / 0x03 round 1
-            // / 0x05 round 2 / 0xFE; state (r, col) is byte 2r + col of the row
-            uint32_t q[4];
+                const int wi = r0 >> 5;
+                uint32_t xw = 0;
+                if (moves) {
+                    uint32_t pw = npre;
+                    if (!single) {
+                        pw = 0;
 #pragma unroll
-            for (int g = 0; g < 2; ++g) {
-                const uint32_t mc = nibble_bytes((capb >> (4 * g)) & 0xFu);
-                const uint32_t ms = nibble_bytes((seedb >> (4 * g)) & 0xFu);
-                const uint32_t m1 = nibble_bytes((a1 >> (4 * g)) & 0xFu);
-                const uint32_t m2 = nibble_bytes((a2 >> (4 * g)) & 0xFu);
-                const uint32_t c0 = (mc & 0x01010101u) | (ms & 0x03030303u) | (~(mc | ms) & 0xFEFEFEFEu);
-                const uint32_t c1 = (mc & 0x01010101u) | (m1 & 0x03030303u) | (m2 & 0x05050505u) |
-                                    (~(mc | m1 | m2) & 0xFEFEFEFEu);
-                q[2 * g] = __byte_perm(c0, c1, 0x5140);
-                q[2 * g + 1] = __byte_perm(c0, c1, 0x7362);
+                        for (int i = 0; i < K - 1; ++i) pw |= CR_LDG(&nbr[c[i] * rwp + wi]);
+                    }
+                    xw = pw | CR_LDG(&nbr[cl * rwp + wi]);
+                }
+                seedb = (xw >> (r0 & 31)) & 0xFFu & ~capb;
+                const uint32_t validb = n - r0 >= 8 ? 0xFFu : ((1u << (n - r0)) - 1u);
+                // every slot of r in M0 (comp) / some slot of r not a cop (deep)
+                Cov8<W> x, e, t, fr;
+                if (single) {
+                    x = xpre;
+                    e = epre;
+                    fr = f;
+                } else {
+                    fr.load(cover + 2 * plane + (size_t)r0 * W);
+                    x.zero();
+                    e.zero();
+#pragma unroll
+                    for (int i = 0; i < K - 1; ++i) {
+                        t.load(cover + (uint32_t)(c[i] * npad + r0) * W);
+                        x.orr(t);
+                        t.load(cover + plane + (uint32_t)(c[i] * npad + r0) * W);
+                        e.orr(t);
+                    }
+                }
+                const uint32_t off = (uint32_t)(cl * npad + r0) * W;
+                t.load(cover + plane + off);
+                e.orr(t);
+                if (moves) {
+                    t.load(cover + off);
+                    x.orr(t);
+                } else {
+                    x = e;
+                }
+                // bytes: column 0 = 0x01 cop / 0x03 seed / 0xFE; column 1 = 0x01 cop / 0x03
+                // round 1 / 0x05 round 2 / 0xFE (0xFE ^ 0xFF, ^ 0xFD, ^ 0xFB); state (r, col) is
+                // byte 2r + col of the row
+                uint32_t q[4], aw = 0, dw = 0;
+                if (W != 1) {
+                    aw = x.eq_bits(fr) & ~capb & validb;
+                    dw = ~e.eq_bits(fr) & 0xFFu;
+                }
+#pragma unroll
+                for (int g = 0; g < 2; ++g) {
+                    const uint32_t mc = nibble_bytes((capb >> (4 * g)) & 0xFu);
+                    const uint32_t ms = nibble_bytes((seedb >> (4 * g)) & 0xFu);
+                    uint32_t m1, m2;
+                    if (W == 1) {
+                        // masks of a slot subset: x == f iff f & ~x is zero, byte by byte
+                        const uint32_t hc = zero_bytes_hi(fr.w[g] & ~x.w[g]);
+                        const uint32_t hd = nonzero_bytes_hi(fr.w[g] & ~e.w[g]);
+                        const uint32_t ma = ((hc >> 7) * 0xFFu) & ~mc & nibble_bytes((validb >> (4 * g)) & 0xFu);
+                        const uint32_t md = (hd >> 7) * 0xFFu;
+                        m2 = ma & md;
+                        m1 = ma & ~md;
+                        a1 |= byte_bits(m1) << (4 * g);
+                        a2 |= byte_bits(m2) << (4 * g);
+                    } else {
+                        const uint32_t b1 = (aw & ~dw) >> (4 * g) & 0xFu, b2 = (aw & dw) >> (4 * g) & 0xFu;
+                        m1 = nibble_bytes(b1);
+                        m2 = nibble_bytes(b2);
+                        a1 |= b1 << (4 * g);
+                        a2 |= b2 << (4 * g);
+                    }
+                    const uint32_t c0 = 0xFEFEFEFEu ^ mc ^ (ms & 0xFDFDFDFDu);
+                    const uint32_t c1 = 0xFEFEFEFEu ^ mc ^ (m1 & 0xFDFDFDFDu) ^ (m2 & 0xFBFBFBFBu);
+                    q[2 * g] = __byte_perm(c0, c1, 0x5140);
+                    q[2 * g + 1] = __byte_perm(c0, c1, 0x7362);
+                }
+                uint8_t* dst = trow + r0 * 2;
+                if (aligned) {
+                    *reinterpret_cast<uint4*>(dst) = make_uint4(q[0], q[1], q[2], q[3]);
+                } else {
+                    for (int b = 0; b < 16 && r0 + (b >> 1) < n; ++b) dst[b] = (uint8_t)(q[b >> 2] >> ((b & 3) * 8));
+                }
+                cnt += __popc(seedb) + __popc(a1) + __popc(a2);
+                any_seed |= seedb;
+                any1 |= a1;
+                any2 |= a2;
             }
-            uint8_t* dst = d.table + (cid * n + r0) * 2;
-            if (aligned) {
-                *reinterpret_cast<uint4*>(dst) = make_uint4(q[0], q[1], q[2], q[3]);
-            } else {
-                for (int b = 0; b < 16 && r0 + (b >> 1) < n; ++b) dst[b] = (uint8_t)(q[b >> 2] >> ((b & 3) * 8));
+            // the 8-bit pieces of four lanes make one word of each row: column-0 marks,
+            // column-1 marks, column-1 frontier slots 0 and 1
+            const uint32_t v = (capb | seedb) | (capb | a1 | a2) << 8 | a1 << 16 | a2 << 24;
+            const uint32_t v1 = __shfl_down_sync(FULL_MASK, v, 1);
+            const uint32_t v2 = __shfl_down_sync(FULL_MASK, v, 2);
+            const uint32_t v3 = __shfl_down_sync(FULL_MASK, v, 3);
+            const uint32_t t01 = __byte_perm(v, v1, 0x5140), t01b = __byte_perm(v, v1, 0x7362);
+            const uint32_t t23 = __byte_perm(v2, v3, 0x5140), t23b = __byte_perm(v2, v3, 0x7362);
+            const int w = it * 8 + (lane >> 2);
+            if ((lane & 3) == 0 && w < rw) {
+                m0row[w] = __byte_perm(t01, t23, 0x5410);
+                m1row[w] = __byte_perm(t01, t23, 0x7632);
+                frow[w] = __byte_perm(t01b, t23b, 0x5410);
+                frow[rwp + w] = __byte_perm(t01b, t23b, 0x7632);
             }
-            wa1[r0 >> 3] = (uint8_t)a1;
-            wa2[r0 >> 3] = (uint8_t)a2;
-            cnt += __popc(a1) + __popc(a2);
-            any1 |= a1;
-            any2 |= a2;
+            changed |= (a1 | a2) != 0u;
         }
-        __syncwarp();
-        // column 1: marked row, frontier row (slot 0 = round 1, slot 1 = round 2), flag
-        uint32_t new1 = 0;
-        if (lane < rwp) {
-            const uint32_t w1 = lane < rw ? reinterpret_cast<const uint32_t*>(wa1)[lane] : 0u;
-            const uint32_t w2 = lane < rw ? reinterpret_cast<const uint32_t*>(wa2)[lane] : 0u;
-            new1 = w1 | w2;
-            d.marked[((size_t)d.C + cid) * rwp + lane] = wcap[lane] | new1;
+        if (padded) {
+            for (int e = rw + lane; e < rwp; e += 32) {
+                m0row[e] = 0u;
+                m1row[e] = 0u;
+                frow[e] = 0u;
+                frow[rwp + e] = 0u;
+            }
+            for (int e = 2 * rwp + lane; e < frow_words; e += 32) frow[e] = 0u;
         }
-        const bool changed = __any_sync(FULL_MASK, new1 != 0u);
-        uint32_t* frow = d.front + ((size_t)d.C + cid) * S * rwp;
-        for (int e = lane; e < S * rwp; e += 32) {
-            const int s = e / rwp, w = e - s * rwp;
-            uint32_t val = 0u;
-            if (s < 2 && w < rw) val = reinterpret_cast<const uint32_t*>(s == 0 ? wa1 : wa2)[w];
-            frow[e] = val;
-        }
+        changed = __any_sync(FULL_MASK, changed);
         if (lane == 0) {
-            d.fflag[cid] = 1;
-            d.fflag[(size_t)d.C + cid] = changed ? 1 : 0;
+            *fl0 = 1;
+            *fl1 = changed ? 1 : 0;
             rows1 += changed ? 1u : 0u;
         }
-        __syncwarp();
     }
     cnt = __reduce_add_sync(FULL_MASK, cnt);
     rows1 = __reduce_add_sync(FULL_MASK, rows1);

@@ -1,8 +1,11 @@
-"""Command line: solve one graph on the GPU, or write a seeded synthetic graph.
+"""Command line: solve one graph on the GPU, cop numbers of many graphs, or write a seeded
+synthetic graph.
 
   python -m copsandrobbers_gb300.cli solve GRAPH.txt -k 3 -p 1 [--rules v1|v2] [--repeat R]
   python -m copsandrobbers_gb300.cli solve --gen regular4:256:12345 -k 3
   python -m copsandrobbers_gb300.cli gen regular4:256:12345 out.txt
+  python -m copsandrobbers_gb300.cli batch --er 4096:16:128:2024 --kmax 3   (cop numbers)
+  python -m copsandrobbers_gb300.cli batch a.txt b.txt ... --kmax 3
 
 Generator specs: regular4:N:SEED, er:N:MEAN_DEGREE:SEED, delaunay:N:SEED[:MEAN_DEGREE].
 """
@@ -52,6 +55,40 @@ def cmd_solve(args) -> int:
     return 0
 
 
+def er_family(spec: str) -> list:
+    """COUNT:NLO:NHI:SEED -> seeded connected G(n, p) graphs, n ~ U[NLO, NHI], mean degree
+    ~ U[3, 6] (the batched workload's family)."""
+    import numpy as np
+
+    count, n_lo, n_hi, seed = (int(x) for x in spec.split(":"))
+    rng = np.random.default_rng(seed)
+    return [G.erdos_renyi(int(rng.integers(n_lo, n_hi + 1)), float(rng.uniform(3, 6)),
+                          G.sub_seed(seed, i) & 0xFFFFFFFF) for i in range(count)]
+
+
+def cmd_batch(args) -> int:
+    from .solver import Context, batch_solve
+
+    graphs = [G.load_matrix(f) for f in args.graphs]
+    if args.er:
+        graphs += er_family(args.er)
+    if not graphs:
+        raise SystemExit("batch needs graph files or --er COUNT:NLO:NHI:SEED")
+    with Context(args.device) as ctx:
+        out = batch_solve(ctx, graphs, args.kmax, 1, args.threads)
+    st = out.stats
+    hist = [0] * (args.kmax + 1)
+    for c in out.cop_numbers:
+        hist[c] += 1
+    print(f"{len(graphs)} graphs, kmax {args.kmax}: {st.ms:.3f} ms, {st.states} states, "
+          f"{st.states / max(st.ms, 1e-9) / 1e6:.3f} G states/s, {st.ctas} CTAs x {st.threads} threads")
+    print("cop numbers (0 = above kmax):", {i: h for i, h in enumerate(hist) if h})
+    if args.list:
+        for i, c in enumerate(out.cop_numbers):
+            print(i, graphs[i].n, c)
+    return 0
+
+
 def cmd_gen(args) -> int:
     G.save_matrix(graph_from_spec(args.spec), args.out)
     return 0
@@ -71,6 +108,14 @@ def main(argv=None) -> int:
     s.add_argument("--profile", action="store_true")
     s.add_argument("--digest", action="store_true")
     s.set_defaults(fn=cmd_solve)
+    b = sub.add_parser("batch")
+    b.add_argument("graphs", nargs="*")
+    b.add_argument("--er")
+    b.add_argument("--kmax", type=int, default=3)
+    b.add_argument("--threads", type=int, default=0, help="threads per CTA (0 = autotune)")
+    b.add_argument("--device", type=int, default=0)
+    b.add_argument("--list", action="store_true")
+    b.set_defaults(fn=cmd_batch)
     g = sub.add_parser("gen")
     g.add_argument("spec")
     g.add_argument("out")

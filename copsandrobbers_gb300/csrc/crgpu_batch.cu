@@ -54,7 +54,14 @@ struct BatchDev {
     int* next;
     int32_t* cop;
     cr_batch_result* res;
+    unsigned long long* cta_time;  // per block: globaltimer at start and after its last graph
 };
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 // 64-bit mixer (the splitmix64 finaliser of Steele, Lea and Flood) used by the table digest.
 __host__ __device__ inline uint64_t mix64(uint64_t z) {
@@ -319,11 +326,14 @@ __device__ int solve_job_k(const BatchDev& b, unsigned char* slot, int gi, int j
     return solve_job<K, 4, P1>(b, slot, gi, jr, sh);
 }
 
-template <bool P1>
-__global__ void __launch_bounds__(512) k_batch(BatchDev b) {
+// Two builds: up to 512 threads per block with up to 128 registers (no spills in the bodies),
+// and 1024 threads with 64 (a few spills, twice the threads on each graph).
+template <bool P1, int MAXT>
+__global__ void __launch_bounds__(MAXT, 1) k_batch(BatchDev b) {
     __shared__ uint64_t sh[32];
     __shared__ int s_job;
     unsigned char* slot = b.slots + (size_t)blockIdx.x * b.slot_bytes;
+    if (threadIdx.x == 0) b.cta_time[2 * blockIdx.x] = b.cta_time[2 * blockIdx.x + 1] = global_ns();
     for (;;) {
         if (threadIdx.x == 0) s_job = atomicAdd(b.next, 1);
         __syncthreads();
@@ -340,7 +350,10 @@ __global__ void __launch_bounds__(512) k_batch(BatchDev b) {
             else win = solve_job_k<3, P1>(b, slot, gi, jr, sh);
             if (win) { cop = k; break; }
         }
-        if (threadIdx.x == 0) b.cop[gi] = cop;
+        if (threadIdx.x == 0) {
+            b.cop[gi] = cop;
+            b.cta_time[2 * blockIdx.x + 1] = global_ns();
+        }
     }
 }
 
@@ -416,10 +429,11 @@ struct BatchInputs {
 
 int launch_batch(cr_context* ctx, const BatchInputs& in, const std::vector<int32_t>& order, int kmax,
                  int p, Shape shape, size_t slot_bytes, std::vector<int32_t>* cop,
-                 std::vector<cr_batch_result>* res, float* ms) {
+                 std::vector<cr_batch_result>* res, float* ms,
+                 std::vector<unsigned long long>* times = nullptr) {
     const int count = (int)order.size();
     const int nblocks = std::max(1, std::min(count, ctx->num_sms * shape.per_sm));
-    void* bufs[12] = {};
+    void* bufs[13] = {};
     auto cleanup = [&]() {
         for (void* q : bufs)
             if (q) cudaFree(q);
@@ -428,12 +442,12 @@ int launch_batch(cr_context* ctx, const BatchInputs& in, const std::vector<int32
     b.count = count;
     b.kmax = kmax;
     b.p = p;
-    size_t sizes[12] = {order.size() * 4, in.n.size() * 4, in.maxdeg.size() * 4, in.rp_off.size() * 8,
+    size_t sizes[13] = {order.size() * 4, in.n.size() * 4, in.maxdeg.size() * 4, in.rp_off.size() * 8,
                         in.col_off.size() * 8, in.rp.size() * 4, std::max<size_t>(in.col.size(), 1) * 2,
                         in.rrp.size() * 4, std::max<size_t>(in.rcol.size(), 1) * 2,
                         (size_t)nblocks * slot_bytes, sizeof(int) + in.n.size() * 4,
-                        in.n.size() * kmax * sizeof(cr_batch_result)};
-    for (int i = 0; i < 12; ++i) {
+                        in.n.size() * kmax * sizeof(cr_batch_result), (size_t)nblocks * 16};
+    for (int i = 0; i < 13; ++i) {
         cudaError_t e = cudaMalloc(&bufs[i], sizes[i]);
         if (e != cudaSuccess) {
             cleanup();
@@ -463,6 +477,7 @@ int launch_batch(cr_context* ctx, const BatchInputs& in, const std::vector<int32
     b.next = (int*)bufs[10];
     b.cop = (int32_t*)((char*)bufs[10] + sizeof(int));
     b.res = (cr_batch_result*)bufs[11];
+    b.cta_time = (unsigned long long*)bufs[12];
     cudaMemsetAsync(bufs[10], 0, sizes[10], st);
     cudaMemsetAsync(bufs[11], 0, sizes[11], st);
     const size_t sm = batch_smem(shape.threads, in.max_n);
@@ -472,10 +487,11 @@ int launch_batch(cr_context* ctx, const BatchInputs& in, const std::vector<int32
     // the batch launch is captured once as a CUDA graph and replayed
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    cudaFuncSetAttribute(k_batch<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    void (*kern)(BatchDev) = shape.threads > 512 ? k_batch<true, 1024> : k_batch<true, 512>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        k_batch<true><<<nblocks, shape.threads, sm, st>>>(b);
+        kern<<<nblocks, shape.threads, sm, st>>>(b);
         e = cudaStreamEndCapture(st, &graph);
     }
     if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
@@ -492,6 +508,10 @@ int launch_batch(cr_context* ctx, const BatchInputs& in, const std::vector<int32
         res->resize(in.n.size() * kmax);
         cudaMemcpy(cop->data(), b.cop, in.n.size() * 4, cudaMemcpyDeviceToHost);
         e = cudaMemcpy(res->data(), b.res, sizes[11], cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess && times) {
+            times->resize((size_t)nblocks * 2);
+            e = cudaMemcpy(times->data(), b.cta_time, sizes[12], cudaMemcpyDeviceToHost);
+        }
     }
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
@@ -515,8 +535,8 @@ int cr_batch_solve(cr_context* ctx, const cr_graph* graphs, int32_t count, int32
     if (!ctx || !graphs || count <= 0 || !cop_number || !results) return CR_ERR_INVALID;
     if (kmax < 1 || kmax > kBatchMaxK) return fail(ctx, CR_ERR_LIMIT, "batch: kmax outside 1..3");
     if (p != 1) return fail(ctx, CR_ERR_LIMIT, "batch: full visibility (p = 1) only");
-    if (threads_per_cta != 0 && threads_per_cta != 256 && threads_per_cta != 512)
-        return fail(ctx, CR_ERR_INVALID, "batch: threads_per_cta must be 0 (autotune), 256 or 512");
+    if (threads_per_cta != 0 && threads_per_cta != 256 && threads_per_cta != 512 && threads_per_cta != 1024)
+        return fail(ctx, CR_ERR_INVALID, "batch: threads_per_cta must be 0 (autotune), 256, 512 or 1024");
     cudaSetDevice(ctx->device);
     BatchInputs in;
     in.n.resize(count);
@@ -566,7 +586,7 @@ int cr_batch_solve(cr_context* ctx, const cr_graph* graphs, int32_t count, int32
     auto fits = [&](Shape s) {
         return (size_t)std::min(count, ctx->num_sms * s.per_sm) * slot_bytes < free_b / 2;
     };
-    Shape shape{threads_per_cta ? threads_per_cta : 256, 2};
+    Shape shape{threads_per_cta ? threads_per_cta : 512, threads_per_cta == 256 ? 2 : 1};
     if (threads_per_cta == 0) {
         // autotune: time candidate launch shapes on a calibration slice (every 8th graph of
         // the cost order, so the slice has the batch's size mix), once per device and shape
@@ -578,7 +598,9 @@ int cr_batch_solve(cr_context* ctx, const cr_graph* graphs, int32_t count, int32
         } else {
             std::vector<int32_t> calib;
             for (int i = 0; i < count; i += 8) calib.push_back(order[i]);
-            const Shape cands[] = {{256, 2}, {256, 3}, {256, 4}, {512, 1}, {512, 2}};
+            // every shape fits the register file: 256 x 2 and 512 x 1 at 128 registers,
+            // 1024 x 1 at 64
+            const Shape cands[] = {{256, 2}, {512, 1}, {1024, 1}};
             float best = 1e30f;
             for (Shape c : cands) {
                 if (!fits(c)) continue;
@@ -599,7 +621,8 @@ int cr_batch_solve(cr_context* ctx, const cr_graph* graphs, int32_t count, int32
     std::vector<int32_t> cop;
     std::vector<cr_batch_result> res;
     float ms = 0;
-    int rc = launch_batch(ctx, in, order, kmax, p, shape, slot_bytes, &cop, &res, &ms);
+    std::vector<unsigned long long> times;
+    int rc = launch_batch(ctx, in, order, kmax, p, shape, slot_bytes, &cop, &res, &ms, &times);
     if (rc) return rc;
     memcpy(cop_number, cop.data(), count * sizeof(int32_t));
     memcpy(results, res.data(), res.size() * sizeof(cr_batch_result));
@@ -610,6 +633,26 @@ int cr_batch_solve(cr_context* ctx, const cr_graph* graphs, int32_t count, int32
         stats->threads = shape.threads;
         stats->ctas = std::min(count, ctx->num_sms * shape.per_sm);
         stats->slot_bytes = (int64_t)slot_bytes;
+        // how evenly the blocks were kept busy: mean busy span over the whole span, and the
+        // time from the median block's last graph to the last block's
+        const size_t nb = times.size() / 2;
+        if (nb) {
+            unsigned long long t0 = ~0ull, t1 = 0;
+            std::vector<double> ends(nb);
+            double busy = 0;
+            for (size_t i = 0; i < nb; ++i) {
+                t0 = std::min(t0, times[2 * i]);
+                t1 = std::max(t1, times[2 * i + 1]);
+            }
+            for (size_t i = 0; i < nb; ++i) {
+                busy += (double)(times[2 * i + 1] - times[2 * i]);
+                ends[i] = (double)(times[2 * i + 1] - t0);
+            }
+            std::sort(ends.begin(), ends.end());
+            const double span = (double)(t1 - t0);
+            stats->busy_frac = span > 0 ? busy / (span * nb) : 0;
+            stats->tail_ms = (span - ends[nb / 2]) / 1e6;
+        }
     }
     for (const auto& r : res)
         if (r.solved && r.status != CR_OK) return fail(ctx, CR_ERR_INTERNAL, "batch: a solve reported a device error");

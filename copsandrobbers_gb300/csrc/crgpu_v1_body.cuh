@@ -617,6 +617,7 @@ __device__ CR_BODY_INLINE void cop_pull_body(const V1Dev& d, int col, int nx, un
     const uint32_t* CR_RESTRICT rp = d.g.row_ptr;
     const uint16_t* CR_RESTRICT adj = d.g.col;
     const bool vec4 = (rwp & 3) == 0;
+    const bool spec = (unsigned long long)mi.rows * 2 >= d.C;   // at least half the rows flagged
     Tally t;
     const size_t step = (size_t)nwk * (blockDim.x >> 5) * CPW;
     for (size_t cb = ((size_t)wk * (blockDim.x >> 5) + warp) * CPW; cb < d.C; cb += step) {
@@ -679,13 +680,42 @@ __device__ CR_BODY_INLINE void cop_pull_body(const V1Dev& d, int col, int nx, un
                         }
                     }
                 }
-                unsigned live = 0;
+                unsigned ok = 0;
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
                     if (s[u] == 0xFFFFFFFFu) continue;
                     if (s[u] >= d.C) { t.err |= kErrRank; continue; }
-                    if (CR_LDG(&fflag_in[s[u]])) live |= 1u << u;
+                    ok |= 1u << u;
                 }
+                if (spec) {
+                    // most rows are flagged: load flag and row together (one round trip), keep
+                    // the row only if flagged (unflagged rows hold stale marks)
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        if (!((ok >> u) & 1u)) continue;
+                        const uint32_t keep = CR_LDG(&fflag_in[s[u]]) ? 0xFFFFFFFFu : 0u;
+                        const uint32_t* row = fin + (size_t)s[u] * S * rwp;
+                        if (vec4) {
+#pragma unroll
+                            for (int w = 0; w < NWP; w += 4) {
+                                if (w < nwords) {
+                                    const uint4 x = CR_LDG(reinterpret_cast<const uint4*>(row + w));
+                                    acc[w] |= x.x & keep; acc[w + 1] |= x.y & keep;
+                                    acc[w + 2] |= x.z & keep; acc[w + 3] |= x.w & keep;
+                                }
+                            }
+                        } else {
+#pragma unroll
+                            for (int w = 0; w < NWP; ++w)
+                                if (w < nwords) acc[w] |= CR_LDG(row + w) & keep;
+                        }
+                    }
+                    continue;
+                }
+                unsigned live = 0;
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+                    if (((ok >> u) & 1u) && CR_LDG(&fflag_in[s[u]])) live |= 1u << u;
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
                     if (!((live >> u) & 1u)) continue;

@@ -58,7 +58,8 @@ class CrBatchResult(ctypes.Structure):
 
 class CrBatchStats(ctypes.Structure):
     _fields_ = [("ms", ctypes.c_double), ("states", ctypes.c_uint64), ("ctas", ctypes.c_int32),
-                ("threads", ctypes.c_int32), ("slot_bytes", ctypes.c_int64)]
+                ("threads", ctypes.c_int32), ("slot_bytes", ctypes.c_int64), ("busy_frac", ctypes.c_double),
+                ("tail_ms", ctypes.c_double)]
 
 
 class CrRequestResult(ctypes.Structure):

@@ -174,12 +174,15 @@ typedef struct cr_batch_stats {
     int32_t ctas;            /* persistent thread blocks */
     int32_t threads;         /* threads per block */
     int64_t slot_bytes;      /* device memory per block */
+    double busy_frac;        /* mean over blocks of their busy time / the batch's time */
+    double tail_ms;          /* batch time after the median block ran out of graphs */
 } cr_batch_stats;
 
 /* Cop numbers of many graphs (v1 rules, visibility p): for every graph, k = 1..kmax in
  * order, stopping at the first WIN, all in one persistent launch.  cop_number[g] = first
- * winning k or 0; results[g * kmax + k - 1] per solve.  threads_per_cta = 0 lets an autotuner
- * pick the launch shape (cached per device and batch shape).  n <= 128, kmax <= 3, p = 1. */
+ * winning k or 0; results[g * kmax + k - 1] per solve.  threads_per_cta = 256, 512 or 1024, or
+ * 0 to let an autotuner pick the launch shape (cached per device and batch shape).
+ * n <= 128, kmax <= 3, p = 1. */
 int cr_batch_solve(cr_context* ctx, const cr_graph* graphs, int32_t count, int32_t kmax, int32_t p,
                    int32_t threads_per_cta, int32_t* cop_number, cr_batch_result* results,
                    cr_batch_stats* stats);

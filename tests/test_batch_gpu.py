@@ -31,7 +31,7 @@ def single(ctx, g, k):
                 "base_captures": caps, "table": s.states()}
 
 
-@pytest.mark.parametrize("threads", [0, 256, 512])
+@pytest.mark.parametrize("threads", [0, 256, 512, 1024])
 def test_batch_matches_single_solves(gpu_ctx, threads):
     graphs = small_batch(40, 7)
     out = batch_solve(gpu_ctx, graphs, kmax=3, p=1, threads=threads)

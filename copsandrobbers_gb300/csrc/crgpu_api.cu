@@ -21,6 +21,8 @@ void launch_and(const V1Dev& d, int col, bool p1, int grid, cudaStream_t st);
 void launch_prep(const V1Dev& d, int col, int nx, int grid, cudaStream_t st);
 void launch_init(const V1Dev& d, int grid, cudaStream_t st);
 void launch_init_pass1(const V1Dev& d, int grid, cudaStream_t st);
+void launch_pass_end(const unsigned long long* counters, unsigned long long* hist, int* idx, int cap,
+                     const unsigned* err, cudaGraphConditionalHandle loop, cudaStream_t st);
 void launch_verdict(const V1Dev& d, int cols, unsigned long long* best, int grid, cudaStream_t st);
 void launch_popcount(const uint32_t* plane, size_t words, unsigned long long* out, int grid,
                      cudaStream_t st);
@@ -77,6 +79,11 @@ struct cr_solver {
     uint64_t n_trans = 0;
     unsigned long long* h_pinned = nullptr;  // pinned read-back slot for the pass counter
     cudaGraphExec_t pass_graph = nullptr;
+    // mainLoop on the device: a graph whose WHILE node replays one pass until a pass finds
+    // nothing; the pass counts land in d_hist, their number in d_hist_n
+    cudaGraphExec_t run_graph = nullptr;
+    unsigned long long* d_hist = nullptr;
+    int* d_hist_n = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evc0 = nullptr, evc1 = nullptr;
     // phase state
     bool initialized = false;
@@ -224,13 +231,20 @@ uint64_t cr_solver_footprint(int32_t n, int32_t k, int32_t p, int32_t rules) {
     b += (uint64_t)cols * C;                             // flags
     b += C * (uint64_t)k * 2;                            // configs
     b += (uint64_t)n * rwp * 4 * 3 + (uint64_t)k * (n + 1) * 4 + (1u << 16);
-    if (cols == 2) b += (2ull * n + 1) * (uint64_t)((n + 7) & ~7) * 4;   // first-pass cover masks
+    if (cols == 2) b += 2ull * n * (uint64_t)((n + 7) & ~7) * 4;   // first-pass cover masks
+    b += (1u << 16) * 8ull + 256;                                 // device pass-loop history
     return b;
 }
 
 static void free_v1(cr_solver* s) {
     if (s->pass_graph) cudaGraphExecDestroy(s->pass_graph);
     s->pass_graph = nullptr;
+    if (s->run_graph) cudaGraphExecDestroy(s->run_graph);
+    s->run_graph = nullptr;
+    if (s->d_hist) cudaFree(s->d_hist);
+    if (s->d_hist_n) cudaFree(s->d_hist_n);
+    s->d_hist = nullptr;
+    s->d_hist_n = nullptr;
     void* ptrs[] = {s->d_rp, s->d_col, s->d_binom, s->d_configs, s->d_hop, s->d_table,
                     s->d_marked, s->d_front, s->d_fflag, s->d_meta, s->d_counters, s->d_err,
                     s->d_heads, s->d_trans, s->d_cand, s->d_cflag, s->d_rrp, s->d_rcol, s->d_nbr, s->d_iso, s->d_rhop, s->d_cover};
@@ -266,6 +280,7 @@ static V1Dev dev_view(const cr_solver* s) {
     d.g.cover = s->d_cover;
     d.g.cover_w = s->cover_w;
     d.g.npad = s->npad;
+    d.g.nnz = (int)s->h_col.size();
     d.k = s->k;
     d.cols = s->cols;
     d.S = s->S;
@@ -352,24 +367,25 @@ static int alloc_v1(cr_solver* s) {
     CR_CUDA(ctx, cudaMemcpyAsync(s->d_nbr, nbr.data(), nbr.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
     CR_CUDA(ctx, cudaMemcpyAsync(s->d_rrp, rrp.data(), rrp.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
     CR_CUDA(ctx, cudaMemcpyAsync(s->d_rcol, rcol.data(), rcol.size() * 2, cudaMemcpyHostToDevice, ctx->stream));
-    // neighbour-slot masks of the folded first pass (two columns, out-degrees <= 32):
-    // plane 0 [c][r] slots of r in {c} + N(c), plane 1 [c][r] slots of r equal to c,
-    // plane 2 [r] every slot of r; masks of cover_w bytes, rows padded to npad robbers
+    // uncovered-slot masks of the folded first pass (two columns, out-degrees <= 32), bit j
+    // for the j-th out-neighbour of r: plane 0 [c][r] slots of r outside {c} + N(c), plane 1
+    // [c][r] slots of r other than c; masks of cover_w bytes, rows padded to npad robbers
     s->cover_w = 0;
     if (s->cols == 2 && s->maxdeg <= 32) {
         const int W = s->maxdeg <= 8 ? 1 : (s->maxdeg <= 16 ? 2 : 4);
         const int n = s->n, npad = (n + 7) & ~7;
         const size_t plane = (size_t)n * npad;
-        std::vector<uint32_t> m(2 * plane + npad, 0);
+        std::vector<uint32_t> m(2 * plane, 0);
         for (int r = 0; r < n; ++r) {
             const uint32_t e0 = s->h_rp[r], deg = s->h_rp[r + 1] - e0;
-            m[2 * plane + r] = deg == 32 ? 0xFFFFFFFFu : ((1u << deg) - 1u);
+            const uint32_t all = deg == 32 ? 0xFFFFFFFFu : ((1u << deg) - 1u);
+            for (int c = 0; c < n; ++c) m[(size_t)c * npad + r] = m[plane + (size_t)c * npad + r] = all;
             for (uint32_t j = 0; j < deg; ++j) {
                 const int v = s->h_col[e0 + j];
-                m[plane + (size_t)v * npad + r] |= 1u << j;      // slot j of r is the cop v
-                m[(size_t)v * npad + r] |= 1u << j;              // ... and so lies in N[v]
+                m[plane + (size_t)v * npad + r] &= ~(1u << j);   // slot j of r is the cop v
+                m[(size_t)v * npad + r] &= ~(1u << j);           // ... and so lies in N[v]
                 // slot j of r lies in N(c) for every c with v in N(c), i.e. c an in-neighbour of v
-                for (uint32_t f = rrp[v]; f < rrp[v + 1]; ++f) m[(size_t)rcol[f] * npad + r] |= 1u << j;
+                for (uint32_t f = rrp[v]; f < rrp[v + 1]; ++f) m[(size_t)rcol[f] * npad + r] &= ~(1u << j);
             }
         }
         std::vector<uint8_t> bytes(m.size() * W);
@@ -568,7 +584,7 @@ static int materialize_init(cr_solver* s) {
 }
 
 // Enqueue one pass: per column a prep kernel and its producer, then the pass counter copy.
-static int v1_enqueue_pass(cr_solver* s, bool profile) {
+static int v1_enqueue_pass(cr_solver* s, bool profile, bool readback = true) {
     cr_context* ctx = s->ctx;
     cudaStream_t st = ctx->stream;
     V1Dev d = dev_view(s);
@@ -594,7 +610,8 @@ static int v1_enqueue_pass(cr_solver* s, bool profile) {
             s->stats.cop_step_launches += 1;
         }
     }
-    CR_CUDA(ctx, cudaMemcpyAsync(s->h_pinned, s->d_counters, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    if (readback)
+        CR_CUDA(ctx, cudaMemcpyAsync(s->h_pinned, s->d_counters, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     return CR_OK;
 }
 
@@ -669,6 +686,8 @@ static int grow_slots_and_replay(cr_solver* s) {
     s->d_cand = nullptr;
     if (s->pass_graph) cudaGraphExecDestroy(s->pass_graph);
     s->pass_graph = nullptr;
+    if (s->run_graph) cudaGraphExecDestroy(s->run_graph);
+    s->run_graph = nullptr;
     s->S *= 2;
     if (!pull_supported(s->S, s->rwp))
         return fail(ctx, CR_ERR_LIMIT, "row too wide for %d value slots", s->S);
@@ -728,9 +747,105 @@ int cr_solver_pass(cr_solver* s, uint64_t* new_wins) {
     return CR_OK;
 }
 
+static constexpr int kHistCap = 1 << 16;   // passes one device-side loop may run
+
+// The pass loop graph: WHILE (flag) { one pass; k_pass_end }, the flag set by k_pass_end.
+static int build_run_graph(cr_solver* s) {
+    cr_context* ctx = s->ctx;
+    cudaStream_t st = ctx->stream;
+    if (!s->d_hist) {
+        CR_CUDA(ctx, cudaMalloc(&s->d_hist, sizeof(unsigned long long) * kHistCap));
+        CR_CUDA(ctx, cudaMalloc(&s->d_hist_n, sizeof(int)));
+    }
+    cudaGraph_t g = nullptr;
+    CR_CUDA(ctx, cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle loop;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&loop, g, 1, cudaGraphCondAssignDefault);
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = loop;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp);
+    if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(st, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                                            cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        int rc = v1_enqueue_pass(s, false, false);
+        launch_pass_end(s->d_counters, s->d_hist, s->d_hist_n, kHistCap, s->d_err, loop, st);
+        cudaGraph_t body = nullptr;
+        e = cudaStreamEndCapture(st, &body);
+        if (rc) {
+            cudaGraphDestroy(g);
+            return rc;
+        }
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&s->run_graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        s->run_graph = nullptr;
+        return fail(ctx, CR_ERR_CUDA, "pass loop graph: %s", cudaGetErrorString(e));
+    }
+    return CR_OK;
+}
+
+// Passes until the fixed point in one graph launch (v1, not profiling).  Returns CR_OK with
+// the counts appended to pass_counts, or leaves the state for the caller's pass-by-pass loop
+// when the loop stopped on an error bit or a full history.
+static int v1_run_on_device(cr_solver* s) {
+    cr_context* ctx = s->ctx;
+    cudaStream_t st = ctx->stream;
+    if (!s->run_graph) {
+        int rc = build_run_graph(s);
+        if (rc) return rc;
+    }
+    CR_CUDA(ctx, cudaMemsetAsync(s->d_hist_n, 0, sizeof(int), st));
+    CR_CUDA(ctx, cudaEventRecord(s->ev0, st));
+    CR_CUDA(ctx, cudaGraphLaunch(s->run_graph, st));
+    CR_CUDA(ctx, cudaEventRecord(s->ev1, st));
+    int n = 0;
+    unsigned bits = 0;
+    CR_CUDA(ctx, cudaMemcpyAsync(&n, s->d_hist_n, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CR_CUDA(ctx, cudaMemcpyAsync(&bits, s->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    CR_CUDA(ctx, cudaStreamSynchronize(st));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+    s->stats.main_ms += ms;
+    if (n <= 0 || n > kHistCap) return fail(ctx, CR_ERR_INTERNAL, "pass loop ran %d passes", n);
+    std::vector<unsigned long long> h(n);
+    CR_CUDA(ctx, cudaMemcpy(h.data(), s->d_hist, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost));
+    int per_pass = s->cols + 1;  // prep kernels and the loop's pass end
+    for (int col = 0; col < s->cols; ++col)
+        per_pass += col % 2 == 0 ? cop_launches(0) : (col < s->cols - 1 ? cop_launches(1) : 1);
+    s->stats.kernel_launches += (int64_t)per_pass * n;
+    if (bits & kErrRank) return fail(ctx, CR_ERR_INTERNAL, "successor rank out of range");
+    if (bits & kErrSlot) {
+        // the last pass overflowed its value slots: keep the passes before it, widen the slots
+        // and replay them; the caller continues pass by pass
+        for (int i = 0; i + 1 < n; ++i) s->pass_counts.push_back(h[i]);
+        return grow_slots_and_replay(s);
+    }
+    for (int i = 0; i < n; ++i) s->pass_counts.push_back(h[i]);
+    s->stats.passes = (int)s->pass_counts.size();
+    if (h[n - 1] == 0) s->finished = true;
+    return CR_OK;
+}
+
 int cr_solver_run(cr_solver* s, uint64_t* pass_counts, int32_t cap, int32_t* passes) {
     if (!s) return CR_ERR_INVALID;
-    for (int i = 0; i < 1 << 16; ++i) {
+    if (s->initialized && !s->finished && s->rules == CR_RULES_V1 && !s->ctx->profiling) {
+        CR_CUDA(s->ctx, cudaSetDevice(s->ctx->device));
+        if (s->init_pending) {
+            uint64_t f;
+            int rc = cr_solver_pass(s, &f);   // the fused first pass
+            if (rc) return rc;
+        }
+        if (!s->finished) {
+            int rc = v1_run_on_device(s);
+            if (rc) return rc;
+        }
+    }
+    for (int i = 0; i < 1 << 16 && !s->finished; ++i) {
         uint64_t f;
         int rc = cr_solver_pass(s, &f);
         if (rc) return rc;

@@ -33,6 +33,8 @@
 
 namespace crgpu {
 
+size_t and_stage_words(int n, int rwp, int nnz);
+
 using namespace cta;
 
 constexpr int kBatchMaxN = 128;
@@ -55,6 +57,7 @@ struct BatchDev {
     int32_t* cop;
     cr_batch_result* res;
     unsigned long long* cta_time;  // per block: globaltimer at start and after its last graph
+    uint32_t smem_words;           // dynamic shared memory of the launch
 };
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -173,6 +176,12 @@ __device__ int solve_job(const BatchDev& b, unsigned char* slot, int gi, int jr,
     d.meta = reinterpret_cast<ColMeta*>(slot + L.meta);
     d.pass_new = reinterpret_cast<unsigned long long*>(slot + L.counters);
     d.err = reinterpret_cast<unsigned*>(slot + L.err);
+    {
+        // room past the last-column body's lane groups for staging the graph
+        constexpr int CPW = 32 / G;
+        const uint32_t groups = (blockDim.x >> 5) * CPW * and_group_words(S, rwp);
+        d.and_stage_words = b.smem_words > groups ? b.smem_words - groups : 0u;
+    }
     uint32_t* binom = reinterpret_cast<uint32_t*>(slot + L.binom);
     uint32_t* nbr = reinterpret_cast<uint32_t*>(slot + L.nbr);
     uint32_t* iso = reinterpret_cast<uint32_t*>(slot + L.iso);
@@ -425,6 +434,7 @@ struct BatchInputs {
     std::vector<uint32_t> rp, rrp;
     std::vector<uint16_t> col, rcol;
     int max_n = 0;
+    size_t max_stage_words = 0;   // the largest graph staging of the last-column body
 };
 
 int launch_batch(cr_context* ctx, const BatchInputs& in, const std::vector<int32_t>& order, int kmax,
@@ -478,9 +488,10 @@ int launch_batch(cr_context* ctx, const BatchInputs& in, const std::vector<int32
     b.cop = (int32_t*)((char*)bufs[10] + sizeof(int));
     b.res = (cr_batch_result*)bufs[11];
     b.cta_time = (unsigned long long*)bufs[12];
+    b.smem_words = (uint32_t)((batch_smem(shape.threads, in.max_n) + in.max_stage_words * 4) / 4);
     cudaMemsetAsync(bufs[10], 0, sizes[10], st);
     cudaMemsetAsync(bufs[11], 0, sizes[11], st);
-    const size_t sm = batch_smem(shape.threads, in.max_n);
+    const size_t sm = batch_smem(shape.threads, in.max_n) + in.max_stage_words * 4;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -564,6 +575,8 @@ int cr_batch_solve(cr_context* ctx, const cr_graph* graphs, int32_t count, int32
             indeg[g.col_idx[e] + 1]++;
         }
         in.maxdeg[i] = md;
+        in.max_stage_words = std::max(in.max_stage_words,
+                                      and_stage_words(g.n, round_words((g.n + 31) / 32), (int)nnz));
         for (int v = 0; v <= g.n; ++v) in.rp.push_back(g.row_ptr[v]);
         for (uint32_t e = 0; e < nnz; ++e) in.col.push_back(g.col_idx[e]);
         // in-neighbour CSR (ascending sources)

@@ -53,20 +53,23 @@ struct DevGraph {
     const uint32_t* nbr;      // [n][rwp]: out-neighbour masks
     const uint32_t* isolated; // [rwp]: vertices without out-neighbours
     const uint32_t* rhop;     // [n][rwp]: bit r of row u set iff u is in hop(r) (transposed hop)
-    // Neighbour-slot masks for the first pass's closed form (cover_w bytes per mask, 0 = not
+    // Uncovered-slot masks for the first pass's closed form (cover_w bytes per mask, 0 = not
     // built; npad = n rounded up to 8).  Bit j of a mask refers to r's j-th out-neighbour:
-    //   cover[c][r]            bit j set iff that neighbour is c or an out-neighbour of c
-    //   cover[n + c][r]        bit j set iff that neighbour is c
-    //   cover[2n][r]           every slot of r (deg(r) low bits)
+    //   cover[c][r]            bit j set iff that neighbour is neither c nor an out-neighbour of c
+    //   cover[n + c][r]        bit j set iff that neighbour is not c
     const uint8_t* cover;
     int cover_w;
     int npad;
+    int nnz = -1;             // row_ptr[n] when the host knows it (sizes shared-memory staging)
 };
 
 // Everything one v1 solve's kernels touch.
 struct V1Dev {
     DevGraph g;
     int k, cols, S;
+    // words of dynamic shared memory past the last-column body's lane-group area where it may
+    // stage the graph arrays its row tests read (0 = none)
+    uint32_t and_stage_words = 0;
     uint32_t C;
     const uint32_t* binom;    // [k][n + 1]: B[i][x] = C(n - x + k - 1 - i, k - i)
     const uint16_t* configs;  // [C][k]

@@ -77,7 +77,24 @@ __global__ void k_verdict(const uint8_t* __restrict__ table, const uint32_t* __r
     verdict_body(table, m0, C, n, rw, rwp, cols, best, blockIdx.x, gridDim.x);
 }
 
+// End of one pass of a device-side pass loop: append the pass count to the history and keep
+// looping while the pass found something, no error bit is set and the history has room.
+__global__ void k_pass_end(const unsigned long long* counters, unsigned long long* hist, int* idx,
+                           int cap, const unsigned* err, cudaGraphConditionalHandle loop) {
+    const int i = *idx;
+    const unsigned long long f = counters[0];
+    hist[i] = f;
+    *idx = i + 1;
+    cudaGraphSetConditional(loop, (f != 0ull && *err == 0u && i + 1 < cap) ? 1u : 0u);
+}
+
 // ---------------------------------------------------------------- host-side launchers ---
+
+void launch_pass_end(const unsigned long long* counters, unsigned long long* hist, int* idx, int cap,
+                     const unsigned* err, cudaGraphConditionalHandle loop, cudaStream_t st) {
+    k_pass_end<<<1, 1, 0, st>>>(counters, hist, idx, cap, err, loop);
+}
+
 
 // Lanes per configuration: a power of two covering the robber row (at least 4).
 static int group_lanes(int rwp) {
@@ -172,9 +189,24 @@ void launch_cop(const V1Dev& d, int col, int nx, int direct, int grid, cudaStrea
 
 int cop_launches(int direct) { return direct ? 1 : 4; }
 
+// Shared-memory words the last-column body stages the graph in: transposed hop rows, row
+// pointers and neighbour lists.
+size_t and_stage_words(int n, int rwp, int nnz) {
+    return (size_t)n * rwp + n + 1 + (size_t)(nnz + 1) / 2;
+}
+
 template <bool P1>
-static void launch_and_p(const V1Dev& d, int col, int grid, cudaStream_t st) {
-    const size_t sm = and_smem_bytes(d.S, d.g.rwp, d.g.n);
+static void launch_and_p(const V1Dev& d0, int col, int grid, cudaStream_t st) {
+    V1Dev d = d0;
+    size_t sm = and_smem_bytes(d.S, d.g.rwp, d.g.n);
+    d.and_stage_words = 0;
+    if (d.g.nnz >= 0) {
+        const size_t words = and_stage_words(d.g.n, d.g.rwp, d.g.nnz);
+        if (sm + words * 4 <= 48 * 1024) {   // within the default dynamic shared-memory limit
+            d.and_stage_words = (uint32_t)words;
+            sm += words * 4;
+        }
+    }
     switch (group_lanes(d.g.rwp)) {
         case 4: k_and<P1, 4><<<grid, 256, sm, st>>>(d, col); break;
         case 8: k_and<P1, 8><<<grid, 256, sm, st>>>(d, col); break;

@@ -157,10 +157,6 @@ __device__ CR_BODY_INLINE void init_body(const V1Dev& d, int K, unsigned wk, uns
 __device__ __forceinline__ uint32_t nibble_bytes(uint32_t b) {
     return ((b * 0x00204081u) & 0x01010101u) * 0xFFu;
 }
-// The top bit of each byte -> 4 bits (byte i -> bit i).
-__device__ __forceinline__ uint32_t byte_bits(uint32_t m) {
-    return ((((m >> 7) & 0x01010101u) * 0x01020408u) >> 24) & 0xFu;
-}
 
 // Cover masks of 8 consecutive robbers (cover_w = W bytes each), packed in 2W words.
 template <int W>
@@ -183,28 +179,36 @@ struct Cov8 {
             }
         }
     }
+    __device__ __forceinline__ void ones() {
+#pragma unroll
+        for (int q = 0; q < NW; ++q) w[q] = 0xFFFFFFFFu;
+    }
     __device__ __forceinline__ void orr(const Cov8& o) {
 #pragma unroll
         for (int q = 0; q < NW; ++q) w[q] |= o.w[q];
     }
-    // bit j set iff robber j's mask equals o's
-    __device__ __forceinline__ uint32_t eq_bits(const Cov8& o) const {
+    __device__ __forceinline__ void andd(const Cov8& o) {
+#pragma unroll
+        for (int q = 0; q < NW; ++q) w[q] &= o.w[q];
+    }
+    // bit j set iff robber j's mask is zero
+    __device__ __forceinline__ uint32_t zero_bits() const {
         uint32_t b = 0;
         if (W == 1) {
 #pragma unroll
             for (int q = 0; q < 2; ++q) {
-                const uint32_t m = __vcmpeq4(w[q], o.w[q]);
-                b |= (((((m >> 7) & 0x01010101u) * 0x01020408u) >> 24) & 0xFu) << (4 * q);
+                const uint32_t m = ~(((w[q] & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | w[q]) & 0x80808080u;
+                b |= ((((m >> 7) & 0x01010101u) * 0x01020408u) >> 24) << (4 * q);
             }
         } else if (W == 2) {
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                const uint32_t m = __vcmpeq2(w[q], o.w[q]);
+                const uint32_t m = __vcmpeq2(w[q], 0u);
                 b |= (((m >> 15) & 1u) | ((m >> 30) & 2u)) << (2 * q);
             }
         } else {
 #pragma unroll
-            for (int q = 0; q < 8; ++q) b |= (uint32_t)(w[q] == o.w[q]) << q;
+            for (int q = 0; q < 8; ++q) b |= (uint32_t)(w[q] == 0u) << q;
         }
         return b;
     }
@@ -213,6 +217,10 @@ struct Cov8 {
 // The next sorted multiset in lexicographic order (the configuration order).
 template <int K>
 __device__ __forceinline__ void next_multiset(int (&c)[K], int n) {
+    if (c[K - 1] < n - 1) {   // the common step: only the last cop moves on
+        ++c[K - 1];
+        return;
+    }
     int i = 0;   // the rightmost position below n - 1 (registers only: no indexed access)
 #pragma unroll
     for (int j = 1; j < K; ++j)
@@ -226,15 +234,6 @@ __device__ __forceinline__ void next_multiset(int (&c)[K], int n) {
         if (j >= i) c[j] = v;
 }
 
-// Byte-wise tests on 4 packed bytes, exact (no carries between bytes): the top bit of byte i
-// is set iff byte i of z is zero / non-zero.
-__device__ __forceinline__ uint32_t zero_bytes_hi(uint32_t z) {
-    return ~(((z & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | z) & 0x80808080u;
-}
-__device__ __forceinline__ uint32_t nonzero_bytes_hi(uint32_t z) {
-    return (((z & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | z) & 0x80808080u;
-}
-
 // initializeCaptures and the whole first pass of a p = 1 solve (two columns) in one sweep that
 // writes every table byte once.  After initializeCaptures only the captures are marked (round
 // 0, both columns), so the first pass has closed forms:
@@ -244,8 +243,9 @@ __device__ __forceinline__ uint32_t nonzero_bytes_hi(uint32_t z) {
 //          on a column-0 mark, N(r) within M0 = cops | N(cops) (cops alone when some cop cannot
 //          move); its round is 1 + the largest column-0 round among N(r): 2 when some
 //          neighbour is not a cop, else 1.
-// With the cover masks both tests are ORs over the k cops: N(r) lies in M0 iff the OR of
-// cover[c][r] is every slot of r, and N(r) lies in the cops iff the OR of cover[n + c][r] is.
+// With the uncovered-slot masks both tests are ANDs over the k cops: N(r) lies in M0 iff the
+// AND of cover[c][r] (slots of r outside {c} + N(c)) is empty, and N(r) lies in the cops iff
+// the AND of cover[n + c][r] (slots of r other than c) is empty.
 // Column 1's marks form its output frontier (value base 1: slot 0 holds round 1, slot 1
 // round 2).  Column 0's frontier is read only through its flags and range, and every
 // configuration has captures, so every column-0 flag is set.
@@ -259,8 +259,8 @@ template <int K, int W>
 __device__ CR_BODY_INLINE void init_pass1_body(const V1Dev& d, unsigned wk, unsigned nwk) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int n = d.g.n, rw = d.g.rw, rwp = d.g.rwp, S = d.S, npad = d.g.npad;
-    const uint32_t* CR_RESTRICT rp = d.g.row_ptr;
     const uint32_t* CR_RESTRICT nbr = d.g.nbr;
+    const uint32_t* CR_RESTRICT iso = d.g.isolated;
     const uint8_t* CR_RESTRICT cover = d.g.cover;
     const size_t plane = (size_t)n * npad * W;          // bytes of one cover plane
     const bool aligned = (n & 7) == 0, single = n <= 256;
@@ -275,16 +275,19 @@ __device__ CR_BODY_INLINE void init_pass1_body(const V1Dev& d, unsigned wk, unsi
 #pragma unroll
         for (int i = 0; i < K; ++i) c[i] = CR_LDG(&d.configs[cb * K + i]);
     }
-    // state of the cops c[0 .. K-2], kept while they stay put (single-block rows only)
+    // state of the cops c[0 .. K-2], kept while they stay put (single-block rows only):
+    // AND of their uncovered masks, their out-neighbours (word lane/4), their bits among this
+    // lane's robbers, and whether all of them can move
     int pre[K > 1 ? K - 1 : 1];
 #pragma unroll
     for (int i = 0; i < K - 1; ++i) pre[i] = -1;
-    Cov8<W> xpre, epre, f;
+    Cov8<W> zpre, znpre;
     bool mpre = true;
-    uint32_t npre = 0;                                   // their out-neighbours, word lane/4
-    xpre.zero();
-    epre.zero();
-    if (single && lane * 8 < n) f.load(cover + 2 * plane + (size_t)lane * 8 * W);
+    uint32_t npre = 0, cpre = 0;
+    zpre.ones();
+    znpre.ones();
+    const int lr0 = lane * 8;                            // this lane's robbers in block 0
+    const uint32_t lvalid = n - lr0 >= 8 ? 0xFFu : (lr0 < n ? (1u << (n - lr0)) - 1u : 0u);
     // row pointers advanced per configuration (no per-row index arithmetic)
     uint8_t* trow = d.table + cb * n * 2;
     uint32_t* m0row = d.marked + cb * rwp;
@@ -301,105 +304,85 @@ __device__ CR_BODY_INLINE void init_pass1_body(const V1Dev& d, unsigned wk, unsi
 #pragma unroll
         for (int i = 0; i < K - 1; ++i) same &= pre[i] == c[i];
         if (!same) {
-            // the leading cops moved: rebuild their masks
-            xpre.zero();
-            epre.zero();
+            // the leading cops moved: rebuild their state
+            zpre.ones();
+            znpre.ones();
             mpre = true;
             npre = 0;
+            cpre = 0;
 #pragma unroll
             for (int i = 0; i < K - 1; ++i) {
                 pre[i] = c[i];
-                mpre &= CR_LDG(&rp[c[i] + 1]) > CR_LDG(&rp[c[i]]);
-                if (single && lane * 8 < n) {
+                mpre &= !((CR_LDG(&iso[c[i] >> 5]) >> (c[i] & 31)) & 1u);
+                if (single && lr0 < n) {
                     npre |= CR_LDG(&nbr[c[i] * rwp + (lane >> 2)]);
+                    const unsigned dv = (unsigned)(c[i] - lr0);
+                    if (dv < 8u) cpre |= 1u << dv;
                     Cov8<W> t;
-                    t.load(cover + (uint32_t)(c[i] * npad + lane * 8) * W);
-                    xpre.orr(t);
-                    t.load(cover + plane + (uint32_t)(c[i] * npad + lane * 8) * W);
-                    epre.orr(t);
+                    t.load(cover + (uint32_t)(c[i] * npad + lr0) * W);
+                    zpre.andd(t);
+                    t.load(cover + plane + (uint32_t)(c[i] * npad + lr0) * W);
+                    znpre.andd(t);
                 }
             }
         }
-        const bool moves = mpre && CR_LDG(&rp[cl + 1]) > CR_LDG(&rp[cl]);
+        const bool moves = mpre && !((CR_LDG(&iso[cl >> 5]) >> (cl & 31)) & 1u);
         bool changed = false;
-        for (int r0 = lane * 8, it = 0; it * 256 < n; r0 += 256, ++it) {
+        for (int r0 = lr0, it = 0; it * 256 < n; r0 += 256, ++it) {
             uint32_t capb = 0, seedb = 0, a1 = 0, a2 = 0;
             if (r0 < n) {
-#pragma unroll
-                for (int i = 0; i < K; ++i) {
-                    const unsigned dv = (unsigned)(c[i] - r0);
-                    if (dv < 8u) capb |= 1u << dv;
-                }
                 const int wi = r0 >> 5;
-                uint32_t xw = 0;
-                if (moves) {
-                    uint32_t pw = npre;
-                    if (!single) {
-                        pw = 0;
-#pragma unroll
-                        for (int i = 0; i < K - 1; ++i) pw |= CR_LDG(&nbr[c[i] * rwp + wi]);
-                    }
-                    xw = pw | CR_LDG(&nbr[cl * rwp + wi]);
-                }
-                seedb = (xw >> (r0 & 31)) & 0xFFu & ~capb;
-                const uint32_t validb = n - r0 >= 8 ? 0xFFu : ((1u << (n - r0)) - 1u);
-                // every slot of r in M0 (comp) / some slot of r not a cop (deep)
-                Cov8<W> x, e, t, fr;
+                uint32_t xw = 0, validb = lvalid;
+                Cov8<W> z, zn, t;
+                const uint32_t off = (uint32_t)(cl * npad + r0) * W;
                 if (single) {
-                    x = xpre;
-                    e = epre;
-                    fr = f;
+                    const unsigned dv = (unsigned)(cl - r0);
+                    capb = cpre | (dv < 8u ? 1u << dv : 0u);
+                    if (moves) xw = npre | CR_LDG(&nbr[cl * rwp + wi]);
+                    z = zpre;
+                    zn = znpre;
                 } else {
-                    fr.load(cover + 2 * plane + (size_t)r0 * W);
-                    x.zero();
-                    e.zero();
+                    validb = n - r0 >= 8 ? 0xFFu : ((1u << (n - r0)) - 1u);
+#pragma unroll
+                    for (int i = 0; i < K; ++i) {
+                        const unsigned dv = (unsigned)(c[i] - r0);
+                        if (dv < 8u) capb |= 1u << dv;
+                        if (moves) xw |= CR_LDG(&nbr[c[i] * rwp + wi]);
+                    }
+                    z.ones();
+                    zn.ones();
 #pragma unroll
                     for (int i = 0; i < K - 1; ++i) {
                         t.load(cover + (uint32_t)(c[i] * npad + r0) * W);
-                        x.orr(t);
+                        z.andd(t);
                         t.load(cover + plane + (uint32_t)(c[i] * npad + r0) * W);
-                        e.orr(t);
+                        zn.andd(t);
                     }
                 }
-                const uint32_t off = (uint32_t)(cl * npad + r0) * W;
+                seedb = (xw >> (r0 & 31)) & 0xFFu & ~capb;
                 t.load(cover + plane + off);
-                e.orr(t);
+                zn.andd(t);
                 if (moves) {
                     t.load(cover + off);
-                    x.orr(t);
+                    z.andd(t);
                 } else {
-                    x = e;
+                    z = zn;
                 }
+                // every slot of r in M0 (comp) / some slot of r not a cop (deep)
+                const uint32_t a = z.zero_bits() & ~capb & validb;
+                const uint32_t deepb = ~zn.zero_bits();
+                a2 = a & deepb;
+                a1 = a & ~deepb;
                 // bytes: column 0 = 0x01 cop / 0x03 seed / 0xFE; column 1 = 0x01 cop / 0x03
                 // round 1 / 0x05 round 2 / 0xFE (0xFE ^ 0xFF, ^ 0xFD, ^ 0xFB); state (r, col) is
                 // byte 2r + col of the row
-                uint32_t q[4], aw = 0, dw = 0;
-                if (W != 1) {
-                    aw = x.eq_bits(fr) & ~capb & validb;
-                    dw = ~e.eq_bits(fr) & 0xFFu;
-                }
+                uint32_t q[4];
 #pragma unroll
                 for (int g = 0; g < 2; ++g) {
                     const uint32_t mc = nibble_bytes((capb >> (4 * g)) & 0xFu);
                     const uint32_t ms = nibble_bytes((seedb >> (4 * g)) & 0xFu);
-                    uint32_t m1, m2;
-                    if (W == 1) {
-                        // masks of a slot subset: x == f iff f & ~x is zero, byte by byte
-                        const uint32_t hc = zero_bytes_hi(fr.w[g] & ~x.w[g]);
-                        const uint32_t hd = nonzero_bytes_hi(fr.w[g] & ~e.w[g]);
-                        const uint32_t ma = ((hc >> 7) * 0xFFu) & ~mc & nibble_bytes((validb >> (4 * g)) & 0xFu);
-                        const uint32_t md = (hd >> 7) * 0xFFu;
-                        m2 = ma & md;
-                        m1 = ma & ~md;
-                        a1 |= byte_bits(m1) << (4 * g);
-                        a2 |= byte_bits(m2) << (4 * g);
-                    } else {
-                        const uint32_t b1 = (aw & ~dw) >> (4 * g) & 0xFu, b2 = (aw & dw) >> (4 * g) & 0xFu;
-                        m1 = nibble_bytes(b1);
-                        m2 = nibble_bytes(b2);
-                        a1 |= b1 << (4 * g);
-                        a2 |= b2 << (4 * g);
-                    }
+                    const uint32_t m1 = nibble_bytes((a1 >> (4 * g)) & 0xFu);
+                    const uint32_t m2 = nibble_bytes((a2 >> (4 * g)) & 0xFu);
                     const uint32_t c0 = 0xFEFEFEFEu ^ mc ^ (ms & 0xFDFDFDFDu);
                     const uint32_t c1 = 0xFEFEFEFEu ^ mc ^ (m1 & 0xFDFDFDFDu) ^ (m2 & 0xFBFBFBFBu);
                     q[2 * g] = __byte_perm(c0, c1, 0x5140);
@@ -980,9 +963,28 @@ __device__ CR_BODY_INLINE void and_body(const V1Dev& d, int col, unsigned wk, un
     uint32_t* wtouch = wmc + rwp;
     uint32_t* wnew = wtouch + rwp;
     const uint8_t* CR_RESTRICT fflag0 = d.fflag;
-    const uint32_t* CR_RESTRICT rp = d.g.row_ptr;
-    const uint16_t* CR_RESTRICT adj = d.g.col;
-    const int avg_deg = max(1, (int)((CR_LDG(&rp[n]) + n - 1) / n));
+    // the row tests' graph arrays (transposed hop rows, CSR), staged in shared memory when
+    // the launch left room for them; read through generic pointers either way
+    const uint32_t* rp = d.g.row_ptr;
+    const uint16_t* adj = d.g.col;
+    const uint32_t* rhop = d.g.rhop;
+    const int nnz = (int)rp[n];
+    if (d.and_stage_words) {
+        const uint32_t need = (uint32_t)(n * rwp + n + 1) + (uint32_t)(nnz + 1) / 2;
+        if (need <= d.and_stage_words) {
+            uint32_t* st = sm + (blockDim.x >> 5) * CPW * per_grp;
+            uint32_t* srp = st + n * rwp;
+            uint16_t* sadj = reinterpret_cast<uint16_t*>(srp + n + 1);
+            for (int i = threadIdx.x; i < n * rwp; i += blockDim.x) st[i] = rhop[i];
+            for (int i = threadIdx.x; i <= n; i += blockDim.x) srp[i] = rp[i];
+            for (int i = threadIdx.x; i < nnz; i += blockDim.x) sadj[i] = adj[i];
+            __syncthreads();
+            rhop = st;
+            rp = srp;
+            adj = sadj;
+        }
+    }
+    const int avg_deg = max(1, (nnz + n - 1) / n);
     Tally t;
     const size_t stride = (size_t)nwk * blockDim.x;
     for (size_t base = (size_t)wk * blockDim.x + warp * 32; base < d.C; base += stride) {
@@ -1022,10 +1024,10 @@ __device__ CR_BODY_INLINE void and_body(const V1Dev& d, int col, unsigned wk, un
                     while (mb) {
                         const int v = gl * 32 + __ffs(mb) - 1;
                         mb &= mb - 1;
-                        const uint32_t* row = d.g.rhop + (size_t)v * rwp;
+                        const uint32_t* row = rhop + (size_t)v * rwp;
 #pragma unroll
                         for (int w = 0; w < G; ++w)
-                            if (w < rwp) acc[w] |= CR_LDG(&row[w]);
+                            if (w < rwp) acc[w] |= row[w];
                     }
                 }
                 group_or<G, G>(acc, gl, wtouch, (touch_form && need) ? rwp : 0);
@@ -1044,7 +1046,7 @@ __device__ CR_BODY_INLINE void and_body(const V1Dev& d, int col, unsigned wk, un
                         while (ub) {
                             const int u = w2 * 32 + __ffs(ub) - 1;
                             ub &= ub - 1;
-                            blocked |= CR_LDG(&d.g.rhop[(size_t)u * rwp + gl]);
+                            blocked |= rhop[(size_t)u * rwp + gl];
                         }
                     }
                     cand &= ~blocked;
@@ -1052,7 +1054,7 @@ __device__ CR_BODY_INLINE void and_body(const V1Dev& d, int col, unsigned wk, un
                 while (cand) {
                     const int r = gl * 32 + __ffs(cand) - 1;
                     cand &= cand - 1;
-                    const uint32_t e0 = CR_LDG(&rp[r]), e1 = CR_LDG(&rp[r + 1]);
+                    const uint32_t e0 = rp[r], e1 = rp[r + 1];
                     bool all;
                     int mx = 0;
                     if (P1) {
@@ -1061,13 +1063,13 @@ __device__ CR_BODY_INLINE void and_body(const V1Dev& d, int col, unsigned wk, un
                         } else {
                             all = true;
                             for (uint32_t e = e0; e < e1 && all; ++e) {
-                                const int v = CR_LDG(&adj[e]);
+                                const int v = adj[e];
                                 all = (wm0[v >> 5] >> (v & 31)) & 1u;
                             }
                         }
                         if (all)
                             for (uint32_t e = e0; e < e1; ++e)
-                                mx = max(mx, (int)(trow[(size_t)CR_LDG(&adj[e]) * cols] >> 1));
+                                mx = max(mx, (int)(trow[(size_t)adj[e] * cols] >> 1));
                     } else {
                         const uint32_t* h = d.hop + (size_t)r * rwp;
                         all = true;

@@ -6,6 +6,7 @@ synthetic graph.
   python -m copsandrobbers_gb300.cli gen regular4:256:12345 out.txt
   python -m copsandrobbers_gb300.cli batch --er 4096:16:128:2024 --kmax 3   (cop numbers)
   python -m copsandrobbers_gb300.cli batch a.txt b.txt ... --kmax 3
+  python -m copsandrobbers_gb300.cli game GRAPH.txt -k 3      (perfect game, p = 1)
 
 Generator specs: regular4:N:SEED, er:N:MEAN_DEGREE:SEED, delaunay:N:SEED[:MEAN_DEGREE].
 """
@@ -89,6 +90,24 @@ def cmd_batch(args) -> int:
     return 0
 
 
+def cmd_game(args) -> int:
+    from .solver import Context, Solver, game_lines
+
+    g = graph_from_spec(args.gen) if args.gen else G.load_matrix(args.graph)
+    with Context(args.device) as ctx:
+        with Solver(ctx, g, args.k, 1) as s:
+            s.init()
+            s.run()
+            v = s.verdict()
+            if not v.win:
+                print("RESULT: LOSS. No universal win found.")
+                return 0
+            walk, _ = s.perfect_game()
+            cfg = s.configs().reshape(-1, args.k)
+    print("\n".join(game_lines(cfg, v.best_config, v.capture_plies, walk)))
+    return 0
+
+
 def cmd_gen(args) -> int:
     G.save_matrix(graph_from_spec(args.spec), args.out)
     return 0
@@ -116,13 +135,19 @@ def main(argv=None) -> int:
     b.add_argument("--device", type=int, default=0)
     b.add_argument("--list", action="store_true")
     b.set_defaults(fn=cmd_batch)
+    gm = sub.add_parser("game")
+    gm.add_argument("graph", nargs="?")
+    gm.add_argument("--gen")
+    gm.add_argument("-k", type=int, required=True)
+    gm.add_argument("--device", type=int, default=0)
+    gm.set_defaults(fn=cmd_game)
     g = sub.add_parser("gen")
     g.add_argument("spec")
     g.add_argument("out")
     g.set_defaults(fn=cmd_gen)
     args = ap.parse_args(argv)
-    if args.cmd == "solve" and not (args.graph or args.gen):
-        ap.error("solve needs GRAPH.txt or --gen SPEC")
+    if args.cmd in ("solve", "game") and not (args.graph or args.gen):
+        ap.error(f"{args.cmd} needs GRAPH.txt or --gen SPEC")
     return args.fn(args)
 
 

@@ -21,6 +21,10 @@ void launch_and(const V1Dev& d, int col, bool p1, int grid, cudaStream_t st);
 void launch_prep(const V1Dev& d, int col, int nx, int grid, cudaStream_t st);
 void launch_init(const V1Dev& d, int grid, cudaStream_t st);
 void launch_init_pass1(const V1Dev& d, int grid, cudaStream_t st);
+void launch_game(const uint8_t* table, const uint16_t* configs, const unsigned long long* heads,
+                 const unsigned long long* trans, const uint32_t* rp, const uint16_t* adj, int n, int k,
+                 long long best, int cap, long long* out_c, int* out_r, int* count, int* captured,
+                 cudaStream_t st);
 void launch_pass_end(const unsigned long long* counters, unsigned long long* hist, int* idx, int cap,
                      const unsigned* err, cudaGraphConditionalHandle loop, cudaStream_t st);
 void launch_verdict(const V1Dev& d, int cols, unsigned long long* best, int grid, cudaStream_t st);
@@ -999,6 +1003,43 @@ int cr_solver_build_transitions(cr_solver* s, uint64_t* total) {
         if (bits) return fail(ctx, CR_ERR_LIMIT, "successor fan-out exceeded the builder's buffer");
     }
     if (total) *total = s->n_trans;
+    return CR_OK;
+}
+
+int cr_solver_perfect_game(cr_solver* s, int64_t* configs, int32_t* robbers, int32_t cap,
+                           int32_t* count, int32_t* captured) {
+    if (!s || !configs || !robbers || !count || !captured || cap <= 0) return CR_ERR_INVALID;
+    cr_context* ctx = s->ctx;
+    if (s->rules != CR_RULES_V1 || s->cols != 2)
+        return fail(ctx, CR_ERR_LIMIT, "the perfect game reads two-column (v1, p = 1) tables");
+    if (!s->finished) return fail(ctx, CR_ERR_STATE, "the solve has not reached its fixed point");
+    *count = 0;
+    *captured = 0;
+    cr_verdict v;
+    int rc = cr_solver_verdict(s, &v);
+    if (rc) return rc;
+    if (!v.win) return CR_OK;
+    rc = cr_solver_build_transitions(s, nullptr);
+    if (rc) return rc;
+    cudaStream_t st = ctx->stream;
+    long long* d_c = nullptr;
+    int* d_r = nullptr;
+    CR_CUDA(ctx, cudaMalloc(&d_c, sizeof(long long) * cap + sizeof(int) * (cap + 2)));
+    d_r = reinterpret_cast<int*>(d_c + cap);
+    launch_game(s->d_table, s->d_configs, s->d_heads, s->d_trans, s->d_rp, s->d_col, s->n, s->k,
+                (long long)v.best_config, cap, d_c, d_r, d_r + cap, d_r + cap + 1, st);
+    cudaError_t e = cudaGetLastError();
+    int meta[2] = {0, 0};
+    std::vector<long long> hc(cap);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(meta, d_r + cap, sizeof(meta), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hc.data(), d_c, sizeof(long long) * cap, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(robbers, d_r, sizeof(int) * cap, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(d_c);
+    if (e != cudaSuccess) return fail(ctx, CR_ERR_CUDA, "perfect game: %s", cudaGetErrorString(e));
+    for (int i = 0; i < meta[0] && i < cap; ++i) configs[i] = hc[i];
+    *count = meta[0];
+    *captured = meta[1];
     return CR_OK;
 }
 

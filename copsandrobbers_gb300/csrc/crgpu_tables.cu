@@ -195,4 +195,88 @@ void launch_scan(const unsigned long long* in, unsigned long long* out, uint32_t
     k_exclusive_scan_serial<<<1, 1024, 0, st>>>(in, out, C);
 }
 
+
+// The perfect game of a solved two-column table (util/perfect_game_extractor.py:67-171
+// restated): from the best configuration and the robber vertex with the largest column-0 round,
+// the cops move to the first successor that lands on the robber, else to the first successor
+// with the smallest marked column-1 round; the robber moves to the first neighbour with the
+// largest marked column-0 round; until capture.  One warp: each ply's argmin / argmax runs
+// across the lanes and is resolved in list order.  out_c / out_r get the position after each
+// ply (index 0 = the start); *count the positions written, *captured 1 when the walk ended in
+// a capture.
+__device__ __forceinline__ bool cops_hold(const uint16_t* configs, long long cid, int k, int r) {
+    bool on = false;
+    for (int i = 0; i < k; ++i) on |= configs[cid * k + i] == r;
+    return on;
+}
+
+__global__ void k_game(const uint8_t* __restrict__ table, const uint16_t* __restrict__ configs,
+                       const unsigned long long* __restrict__ heads, const unsigned long long* __restrict__ trans,
+                       const uint32_t* __restrict__ rp, const uint16_t* __restrict__ adj, int n, int k,
+                       long long best, int cap, long long* out_c, int* out_r, int* count, int* captured) {
+    const int lane = threadIdx.x & 31;
+    const int cols = 2;
+    // the robber's start: the first vertex with the largest column-0 round
+    unsigned long long key = ~0ull;
+    for (int r = lane; r < n; r += 32) {
+        const int rnd = table[((size_t)best * n + r) * cols] >> 1;
+        key = min(key, ((unsigned long long)(255 - rnd) << 32) | (unsigned)r);
+    }
+    // smallest (255 - round, vertex): the largest round, first in vertex order
+    unsigned long long kk = key;
+    for (int off = 16; off > 0; off >>= 1) kk = min(kk, __shfl_xor_sync(0xFFFFFFFFu, kk, off));
+    long long cc = best;
+    int rr = (int)(kk & 0xFFFFFFFFu);
+    int m = 0, cap_hit = 0;
+    if (lane == 0) { out_c[0] = cc; out_r[0] = rr; }
+    m = 1;
+    while (m < cap) {
+        if (cops_hold(configs, cc, k, rr)) { cap_hit = 1; break; }
+        // cops: first capture in list order, else the first smallest marked column-1 round
+        const unsigned long long t0 = heads[cc], t1 = heads[cc + 1];
+        unsigned long long bk = ~0ull;
+        for (unsigned long long t = t0 + lane; t < t1; t += 32) {
+            const long long nc = (long long)(trans[t] / (unsigned long long)n);
+            unsigned long long kv;
+            if (cops_hold(configs, nc, k, rr)) {
+                kv = (t - t0);                                   // class 0: capture
+            } else {
+                const uint8_t b = table[((size_t)nc * n + rr) * cols + 1];
+                if (!(b & 1)) continue;
+                kv = (1ull << 62) | ((unsigned long long)(b >> 1) << 32) | (t - t0);
+            }
+            bk = min(bk, kv);
+        }
+        for (int off = 16; off > 0; off >>= 1) bk = min(bk, __shfl_xor_sync(0xFFFFFFFFu, bk, off));
+        if (bk != ~0ull) cc = (long long)(trans[t0 + (bk & 0xFFFFFFFFull)] / (unsigned long long)n);
+        if (lane == 0) { out_c[m] = cc; out_r[m] = rr; }
+        ++m;
+        if (m >= cap) break;
+        if (cops_hold(configs, cc, k, rr)) { cap_hit = 1; break; }
+        // robber: the first neighbour with the largest marked column-0 round
+        unsigned long long rk = ~0ull;
+        for (uint32_t e = rp[rr] + lane; e < rp[rr + 1]; e += 32) {
+            const int v = adj[e];
+            const uint8_t b = table[((size_t)cc * n + v) * cols];
+            if (!(b & 1)) continue;
+            rk = min(rk, ((unsigned long long)(255 - (b >> 1)) << 32) | (e - rp[rr]));
+        }
+        for (int off = 16; off > 0; off >>= 1) rk = min(rk, __shfl_xor_sync(0xFFFFFFFFu, rk, off));
+        if (rk != ~0ull) rr = adj[rp[rr] + (rk & 0xFFFFFFFFull)];
+        if (lane == 0) { out_c[m] = cc; out_r[m] = rr; }
+        ++m;
+    }
+    if (lane == 0) {
+        *count = m;
+        *captured = cap_hit;
+    }
+}
+
+void launch_game(const uint8_t* table, const uint16_t* configs, const unsigned long long* heads,
+                 const unsigned long long* trans, const uint32_t* rp, const uint16_t* adj, int n, int k,
+                 long long best, int cap, long long* out_c, int* out_r, int* count, int* captured,
+                 cudaStream_t st) {
+    k_game<<<1, 32, 0, st>>>(table, configs, heads, trans, rp, adj, n, k, best, cap, out_c, out_r, count, captured);
+}
+
 }  // namespace crgpu

@@ -114,6 +114,9 @@ SIGNATURES = {
                                       ctypes.c_int32, ctypes.c_int32, c_i32p, ctypes.POINTER(CrBatchResult),
                                       ctypes.POINTER(CrBatchStats)]),
     "cr_solver_digest": (ctypes.c_int, [ctypes.c_void_p, c_u64p]),
+    "cr_solver_perfect_game": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64),
+                                              ctypes.POINTER(ctypes.c_int32), ctypes.c_int32,
+                                              ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
     "cr_server_create": (ctypes.c_int, [ctypes.c_int32, ctypes.c_uint64, ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]),
     "cr_server_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(CrGraph), ctypes.c_int32, ctypes.c_int32,
                                         ctypes.c_int32, c_u64p]),

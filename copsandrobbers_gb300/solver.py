@@ -156,6 +156,18 @@ class Solver:
             self.ptr, heads.ctypes.data_as(N.c_u64p), heads.size, data.ctypes.data_as(N.c_u64p), data.size))
         return heads, data[: int(total.value)]
 
+    def perfect_game(self, cap: int = 1024) -> tuple[list, bool]:
+        """The perfect game of a solved p = 1 table (cr_solver_perfect_game): the positions
+        (configuration id, robber vertex) after each ply, starting position first, and whether
+        the walk ended in a capture.  Empty for a LOSS."""
+        cfg = np.zeros(cap, dtype=np.int64)
+        rob = np.zeros(cap, dtype=np.int32)
+        cnt, capt = ctypes.c_int32(), ctypes.c_int32()
+        _check(self.ctx.ptr, N.lib().cr_solver_perfect_game(
+            self.ptr, cfg.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+            rob.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), cap, ctypes.byref(cnt), ctypes.byref(capt)))
+        return [(int(cfg[i]), int(rob[i])) for i in range(cnt.value)], bool(capt.value)
+
     def write_table_file(self, path: str) -> None:
         _check(self.ctx.ptr, N.lib().cr_solver_write_table_file(self.ptr, path.encode()))
 
@@ -195,6 +207,29 @@ def solve(ctx: Context, graph: Graph, k: int, p: int = 1, rules: int = N.CR_RULE
         v = s.verdict()
         st = s.states() if with_states else None
         return Result(st, counts, caps, v, s.stats())
+
+
+def game_lines(configs: np.ndarray, best: int, max_plies: int, positions: list) -> list:
+    """The perfect game as the reference's extractor prints it (util/perfect_game_extractor.py
+    :91-165, from its 'Optimal Cop Start' line on); configs = the [C][k] configuration table."""
+    show = lambda c: str(np.asarray(configs[c], dtype=np.uint8))
+    out = ["", f"Optimal Cop Start: {show(best)} | Max Plys: {max_plies}", "", "--- PERFECT GAME PATH ---"]
+    i = 0
+    while i < len(positions):
+        c, r = positions[i]
+        if r in set(int(x) for x in configs[c]):
+            out.append(f"Ply {i}: Game Over! Robber captured at node {r}.")
+            break
+        out.append(f"Ply {i} [Cop Turn]: Cops at {show(c)} | Robber at {r}")
+        if i + 1 >= len(positions):
+            break
+        c, r = positions[i + 1]
+        if r in set(int(x) for x in configs[c]):
+            out.append(f"Ply {i + 1}: Cops moved to {show(c)} and CAPTURED the robber!")
+            break
+        out.append(f"Ply {i + 1} [Robber Turn]: Cops at {show(c)} | Robber at {r}")
+        i += 2
+    return out
 
 
 def footprint(n: int, k: int, p: int = 1, rules: int = N.CR_RULES_V1) -> int:

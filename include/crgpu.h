@@ -187,6 +187,17 @@ int cr_batch_solve(cr_context* ctx, const cr_graph* graphs, int32_t count, int32
                    int32_t threads_per_cta, int32_t* cop_number, cr_batch_result* results,
                    cr_batch_stats* stats);
 
+/* The perfect game of a solved v1 table with two columns (p = 1), restating the reference's
+ * util/perfect_game_extractor.py:67-171 on the device: from findFinalResult's configuration and
+ * the robber vertex with the largest column-0 round, the cops take the first successor that
+ * lands on the robber, else the first successor with the smallest marked column-1 round; the
+ * robber takes the first neighbour with the largest marked column-0 round; until capture.
+ * configs[i] / robbers[i] = the position after ply i (index 0 = the start), at most cap of
+ * them; *count = positions written; *captured = 1 when the walk ended in a capture.  A LOSS
+ * verdict gives *count = 0.  Needs the fixed point (CR_ERR_STATE before it). */
+int cr_solver_perfect_game(cr_solver* s, int64_t* configs, int32_t* robbers, int32_t cap,
+                           int32_t* count, int32_t* captured);
+
 /* 64-bit digest of a solver's states table: sum over its 8-byte little-endian words w_j
  * (zero-padded) of mix64(w_j ^ (j * 0x9E3779B97F4A7C15)) modulo 2^64, mix64 being the
  * splitmix64 finaliser.  Used to compare batched and single solves without copying tables. */

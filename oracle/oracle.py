@@ -197,6 +197,48 @@ def _verdict(sol: Solution) -> None:
     sol.capture_plies = int(worst.value)
 
 
+def perfect_game(sol: Solution, graph) -> list:
+    """util/perfect_game_extractor.py:67-165 restated over a two-column table: the positions
+    (config id, robber) after each ply, the start first.  Empty for a LOSS."""
+    if not sol.win:
+        return []
+    n, st, cfg = sol.n, sol.states, sol.configs
+    rp, col = graph.csr()
+    rnd = lambda c, r, t: int(st[(c * n + r) * 2 + t]) >> 1
+    marked = lambda c, r, t: bool(st[(c * n + r) * 2 + t] & 1)
+    holds = lambda c, r: r in set(int(x) for x in cfg[c])
+    # robber start: first vertex with the largest column-0 round (:101-107)
+    best_r, most = -1, -1
+    for r in range(n):
+        if rnd(sol.best_config, r, 0) > most:
+            most, best_r = rnd(sol.best_config, r, 0), r
+    c, r = sol.best_config, best_r
+    out = [(c, r)]
+    while len(out) < 4096:
+        if holds(c, r):
+            break
+        nxt, low = c, 999                        # cops (:121-139)
+        for t in range(int(sol.heads[c]), int(sol.heads[c + 1])):
+            nc = int(sol.transitions[t]) // n
+            if holds(nc, r):
+                nxt = nc
+                break
+            if marked(nc, r, 1) and rnd(nc, r, 1) < low:
+                low, nxt = rnd(nc, r, 1), nc
+        c = nxt
+        out.append((c, r))
+        if holds(c, r):
+            break
+        nr, high = r, -1                         # robber (:147-160)
+        for v in col[rp[r]:rp[r + 1]]:
+            v = int(v)
+            if marked(c, v, 0) and rnd(c, v, 0) > high:
+                high, nr = rnd(c, v, 0), v
+        r = nr
+        out.append((c, r))
+    return out
+
+
 # ------------------------------------------------------------- reference binaries --------
 
 RE_PASS = re.compile(r"Pass (\d+): Found (\d+) new winning states")

@@ -53,8 +53,15 @@ struct cr_solver {
     int n = 0, k = 0, p = 0, rules = CR_RULES_V1, cols = 0, rw = 0, rwp = 0, S = 2;
     uint64_t C = 0;
     int maxdeg = 0;
-    std::vector<uint32_t> h_rp;
+    std::vector<uint32_t> h_rp;       // the robber's moves (with self-loops under CR_ROBBER_STAY)
     std::vector<uint16_t> h_col;
+    std::vector<uint32_t> h_crp;      // the cops' moves (with self-loops under CR_COP_STAY)
+    std::vector<uint16_t> h_ccol;
+    bool cop_stay = false, robber_stay = false;
+    int cop_maxdeg = 0;
+    uint32_t* d_crp = nullptr;        // set only when the two move graphs differ
+    uint16_t* d_ccol = nullptr;
+    uint32_t* d_ciso = nullptr;
     std::vector<uint32_t> h_binom;
     // device
     uint32_t* d_rp = nullptr;
@@ -251,7 +258,8 @@ static void free_v1(cr_solver* s) {
     s->d_hist_n = nullptr;
     void* ptrs[] = {s->d_rp, s->d_col, s->d_binom, s->d_configs, s->d_hop, s->d_table,
                     s->d_marked, s->d_front, s->d_fflag, s->d_meta, s->d_counters, s->d_err,
-                    s->d_heads, s->d_trans, s->d_cand, s->d_cflag, s->d_rrp, s->d_rcol, s->d_nbr, s->d_iso, s->d_rhop, s->d_cover};
+                    s->d_heads, s->d_trans, s->d_cand, s->d_cflag, s->d_rrp, s->d_rcol, s->d_nbr, s->d_iso, s->d_rhop, s->d_cover,
+                    s->d_crp, s->d_ccol, s->d_ciso};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     s->d_rp = nullptr; s->d_col = nullptr; s->d_binom = nullptr; s->d_configs = nullptr;
@@ -260,6 +268,7 @@ static void free_v1(cr_solver* s) {
     s->d_heads = nullptr; s->d_trans = nullptr; s->d_cand = nullptr; s->d_cflag = nullptr;
     s->d_rrp = nullptr; s->d_rcol = nullptr; s->d_nbr = nullptr; s->d_iso = nullptr; s->d_rhop = nullptr;
     s->d_cover = nullptr;
+    s->d_crp = nullptr; s->d_ccol = nullptr; s->d_ciso = nullptr;
     if (s->h_pinned) cudaFreeHost(s->h_pinned);
     s->h_pinned = nullptr;
     cudaEvent_t evs[] = {s->ev0, s->ev1, s->evc0, s->evc1};
@@ -285,6 +294,9 @@ static V1Dev dev_view(const cr_solver* s) {
     d.g.cover_w = s->cover_w;
     d.g.npad = s->npad;
     d.g.nnz = (int)s->h_col.size();
+    d.g.cop_row_ptr = s->d_crp;
+    d.g.cop_col = s->d_ccol;
+    d.g.cop_isolated = s->d_ciso;
     d.k = s->k;
     d.cols = s->cols;
     d.S = s->S;
@@ -347,22 +359,37 @@ static int alloc_v1(cr_solver* s) {
                 rhop[(size_t)u * s->rwp + (r >> 5)] |= 1u << (r & 31);
     CR_CUDA(ctx, cudaMalloc(&s->d_rhop, rhop.size() * 4));
     CR_CUDA(ctx, cudaMemcpyAsync(s->d_rhop, rhop.data(), rhop.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
-    // out-neighbour masks (capture-seed closed form) and the in-neighbour CSR (push mode)
+    // the cops' out-neighbour masks (capture-seed closed form) and their in-neighbour CSR
+    // (push mode), both of the cops' move graph
+    const std::vector<uint32_t>& crp = s->h_crp;
+    const std::vector<uint16_t>& ccol = s->h_ccol;
     std::vector<uint32_t> nbr((size_t)s->n * s->rwp, 0);
     std::vector<uint32_t> rrp(s->n + 1, 0);
-    for (uint32_t e = 0; e < s->h_col.size(); ++e) rrp[s->h_col[e] + 1]++;
+    for (uint32_t e = 0; e < ccol.size(); ++e) rrp[ccol[e] + 1]++;
     for (int v = 0; v < s->n; ++v) rrp[v + 1] += rrp[v];
-    std::vector<uint16_t> rcol(std::max<size_t>(s->h_col.size(), 1));
+    std::vector<uint16_t> rcol(std::max<size_t>(ccol.size(), 1));
     std::vector<uint32_t> fill(rrp.begin(), rrp.end() - 1);
     for (int u = 0; u < s->n; ++u)
-        for (uint32_t e = s->h_rp[u]; e < s->h_rp[u + 1]; ++e) {
-            const int v = s->h_col[e];
+        for (uint32_t e = crp[u]; e < crp[u + 1]; ++e) {
+            const int v = ccol[e];
             nbr[(size_t)u * s->rwp + (v >> 5)] |= 1u << (v & 31);
             rcol[fill[v]++] = (uint16_t)u;  // in-neighbours of v, ascending u
         }
-    std::vector<uint32_t> iso(s->rwp, 0);
-    for (int v = 0; v < s->n; ++v)
+    // robbers without a move (the last column's vacuous AND), cops without a move
+    std::vector<uint32_t> iso(s->rwp, 0), ciso(s->rwp, 0);
+    for (int v = 0; v < s->n; ++v) {
         if (s->h_rp[v + 1] == s->h_rp[v]) iso[v >> 5] |= 1u << (v & 31);
+        if (crp[v + 1] == crp[v]) ciso[v >> 5] |= 1u << (v & 31);
+    }
+    if (s->cop_stay != s->robber_stay) {
+        CR_CUDA(ctx, cudaMalloc(&s->d_crp, crp.size() * 4));
+        CR_CUDA(ctx, cudaMalloc(&s->d_ccol, std::max<size_t>(ccol.size(), 1) * 2));
+        CR_CUDA(ctx, cudaMalloc(&s->d_ciso, ciso.size() * 4));
+        CR_CUDA(ctx, cudaMemcpyAsync(s->d_crp, crp.data(), crp.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+        if (!ccol.empty())
+            CR_CUDA(ctx, cudaMemcpyAsync(s->d_ccol, ccol.data(), ccol.size() * 2, cudaMemcpyHostToDevice, ctx->stream));
+        CR_CUDA(ctx, cudaMemcpyAsync(s->d_ciso, ciso.data(), ciso.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+    }
     CR_CUDA(ctx, cudaMalloc(&s->d_iso, iso.size() * 4));
     CR_CUDA(ctx, cudaMemcpyAsync(s->d_iso, iso.data(), iso.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
     CR_CUDA(ctx, cudaMalloc(&s->d_nbr, nbr.size() * 4));
@@ -412,7 +439,10 @@ int cr_solver_create(cr_context* ctx, const cr_graph* g, int32_t k, int32_t p, i
     if (g->n > CR_MAX_N) return fail(ctx, CR_ERR_LIMIT, "n=%d exceeds %d vertices", g->n, CR_MAX_N);
     if (k <= 0 || k > CR_MAX_K) return fail(ctx, CR_ERR_LIMIT, "k=%d outside 1..%d", k, CR_MAX_K);
     if (p <= 0 || p > 63) return fail(ctx, CR_ERR_INVALID, "p=%d outside 1..63", p);
-    if (rules != CR_RULES_V1 && rules != CR_RULES_V2) return fail(ctx, CR_ERR_INVALID, "unknown rules %d", rules);
+    const int stay = rules & (CR_COP_STAY | CR_ROBBER_STAY);
+    const int base_rules = rules & ~(CR_COP_STAY | CR_ROBBER_STAY);
+    if (base_rules != CR_RULES_V1 && base_rules != CR_RULES_V2) return fail(ctx, CR_ERR_INVALID, "unknown rules %d", rules);
+    if (stay && base_rules != CR_RULES_V1) return fail(ctx, CR_ERR_LIMIT, "stay-allowed rules need CR_RULES_V1");
     if (!g->row_ptr || (g->row_ptr[g->n] && !g->col_idx)) return fail(ctx, CR_ERR_INVALID, "graph arrays missing");
     for (int v = 0; v < g->n; ++v)
         if (g->row_ptr[v + 1] < g->row_ptr[v]) return fail(ctx, CR_ERR_INVALID, "row_ptr not monotone");
@@ -426,16 +456,39 @@ int cr_solver_create(cr_context* ctx, const cr_graph* g, int32_t k, int32_t p, i
     s->n = g->n;
     s->k = k;
     s->p = p;
-    s->rules = rules;
+    s->rules = base_rules;
+    rules = base_rules;
+    s->cop_stay = (stay & CR_COP_STAY) != 0;
+    s->robber_stay = (stay & CR_ROBBER_STAY) != 0;
     s->S = slots_for(g->n);
     layout(s->n, k, p, rules, s->S, &s->C, &s->cols, &s->rw, &s->rwp);
     if (s->C == 0 || s->C >= (1ull << 32)) {
         delete s;
         return fail(ctx, CR_ERR_LIMIT, "config count C(%d,%d) outside 1..2^32-1", g->n + k - 1, k);
     }
-    s->h_rp.assign(g->row_ptr, g->row_ptr + g->n + 1);
-    s->h_col.assign(g->col_idx, g->col_idx + g->row_ptr[g->n]);
-    for (int v = 0; v < s->n; ++v) s->maxdeg = std::max<int>(s->maxdeg, s->h_rp[v + 1] - s->h_rp[v]);
+    // the two move graphs: the input graph, plus a self-loop per vertex for a side that may stay
+    auto move_graph = [&](bool self, std::vector<uint32_t>& rp, std::vector<uint16_t>& col) {
+        rp.assign(1, 0);
+        col.clear();
+        for (int v = 0; v < g->n; ++v) {
+            bool placed = !self;
+            for (uint32_t e = g->row_ptr[v]; e < g->row_ptr[v + 1]; ++e) {
+                if (!placed && g->col_idx[e] >= v) {
+                    col.push_back((uint16_t)v);
+                    placed = true;
+                }
+                col.push_back(g->col_idx[e]);
+            }
+            if (!placed) col.push_back((uint16_t)v);
+            rp.push_back((uint32_t)col.size());
+        }
+    };
+    move_graph(s->robber_stay, s->h_rp, s->h_col);
+    move_graph(s->cop_stay, s->h_crp, s->h_ccol);
+    for (int v = 0; v < s->n; ++v) {
+        s->maxdeg = std::max<int>(s->maxdeg, s->h_rp[v + 1] - s->h_rp[v]);
+        s->cop_maxdeg = std::max<int>(s->cop_maxdeg, s->h_crp[v + 1] - s->h_crp[v]);
+    }
     // B[i][x] = C(n - x + k - 1 - i, k - i)
     s->h_binom.assign((size_t)k * (s->n + 1), 0);
     for (int i = 0; i < k; ++i)
@@ -977,14 +1030,16 @@ int cr_solver_build_transitions(cr_solver* s, uint64_t* total) {
     CR_CUDA(ctx, cudaSetDevice(ctx->device));
     cudaStream_t st = ctx->stream;
     if (!s->d_heads) {
-        const int cap = trans_cap(s->k, s->maxdeg);
+        const int cap = trans_cap(s->k, s->cop_maxdeg);
         if (cap > 8192) return fail(ctx, CR_ERR_LIMIT, "successor fan-out %d too large for the CSR builder", cap);
         unsigned long long* counts = nullptr;
         CR_CUDA(ctx, cudaMalloc(&counts, s->C * 8));
         CR_CUDA(ctx, cudaMalloc(&s->d_heads, (s->C + 1) * 8));
         CR_CUDA(ctx, cudaMemsetAsync(s->d_err, 0, sizeof(unsigned), st));
         const int grid = ctx->num_sms * 8;
-        launch_trans(s->k, s->d_configs, (uint32_t)s->C, s->n, s->d_rp, s->d_col, s->d_binom, cap, counts,
+        const uint32_t* trp = s->d_crp ? s->d_crp : s->d_rp;
+        const uint16_t* tcol = s->d_ccol ? s->d_ccol : s->d_col;
+        launch_trans(s->k, s->d_configs, (uint32_t)s->C, s->n, trp, tcol, s->d_binom, cap, counts,
                      nullptr, nullptr, s->d_err, grid, st);
         launch_scan(counts, s->d_heads, (uint32_t)s->C, st);
         CR_CUDA(ctx, cudaGetLastError());
@@ -994,7 +1049,7 @@ int cr_solver_build_transitions(cr_solver* s, uint64_t* total) {
         cudaFree(counts);
         s->n_trans = tot;
         CR_CUDA(ctx, cudaMalloc(&s->d_trans, std::max<uint64_t>(tot, 1) * 8));
-        launch_trans(s->k, s->d_configs, (uint32_t)s->C, s->n, s->d_rp, s->d_col, s->d_binom, cap, nullptr,
+        launch_trans(s->k, s->d_configs, (uint32_t)s->C, s->n, trp, tcol, s->d_binom, cap, nullptr,
                      s->d_heads, s->d_trans, s->d_err, grid, st);
         CR_CUDA(ctx, cudaGetLastError());
         unsigned bits = 0;
@@ -1010,8 +1065,8 @@ int cr_solver_perfect_game(cr_solver* s, int64_t* configs, int32_t* robbers, int
                            int32_t* count, int32_t* captured) {
     if (!s || !configs || !robbers || !count || !captured || cap <= 0) return CR_ERR_INVALID;
     cr_context* ctx = s->ctx;
-    if (s->rules != CR_RULES_V1 || s->cols != 2)
-        return fail(ctx, CR_ERR_LIMIT, "the perfect game reads two-column (v1, p = 1) tables");
+    if (s->rules != CR_RULES_V1 || s->cols != 2 || s->cop_stay || s->robber_stay)
+        return fail(ctx, CR_ERR_LIMIT, "the perfect game reads two-column (v1, p = 1) tables without stays");
     if (!s->finished) return fail(ctx, CR_ERR_STATE, "the solve has not reached its fixed point");
     *count = 0;
     *captured = 0;
@@ -1071,7 +1126,8 @@ int cr_solver_write_table_file(cr_solver* s, const char* path) {
     if (rc) return rc;
     const uint64_t cfg = s->C * (uint64_t)s->k, heads = (s->C + 1) * 8, trans = s->n_trans * 8;
     const uint64_t states = s->C * (uint64_t)s->n * s->cols;
-    uint64_t hdr[12] = {(uint64_t)s->k, (uint64_t)s->n, (uint64_t)s->cols, s->C, states, 1, 0, 0,
+    uint64_t hdr[12] = {(uint64_t)s->k, (uint64_t)s->n, (uint64_t)s->cols, s->C, states, 1,
+                        (uint64_t)s->cop_stay, (uint64_t)s->robber_stay,
                         96, 96 + cfg, 96 + cfg + heads, 96 + cfg + heads + trans};
     FILE* f = fopen(path, "wb");
     if (!f) return fail(ctx, CR_ERR_IO, "cannot open %s for writing", path);

@@ -61,7 +61,17 @@ struct DevGraph {
     int cover_w;
     int npad;
     int nnz = -1;             // row_ptr[n] when the host knows it (sizes shared-memory staging)
+    // The cops' move graph when it differs from the robber's (row_ptr / col above), i.e. under
+    // the stay-allowed rules; null = the same graph.  rrow_ptr / rcol and nbr always describe
+    // the cops' moves.
+    const uint32_t* cop_row_ptr = nullptr;
+    const uint16_t* cop_col = nullptr;
+    const uint32_t* cop_isolated = nullptr;
 };
+
+__host__ __device__ inline const uint32_t* cop_rows(const DevGraph& g) { return g.cop_row_ptr ? g.cop_row_ptr : g.row_ptr; }
+__host__ __device__ inline const uint16_t* cop_cols(const DevGraph& g) { return g.cop_col ? g.cop_col : g.col; }
+__host__ __device__ inline const uint32_t* cop_iso(const DevGraph& g) { return g.cop_isolated ? g.cop_isolated : g.isolated; }
 
 // Everything one v1 solve's kernels touch.
 struct V1Dev {

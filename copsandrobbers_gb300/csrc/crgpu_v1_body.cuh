@@ -260,7 +260,7 @@ __device__ CR_BODY_INLINE void init_pass1_body(const V1Dev& d, unsigned wk, unsi
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int n = d.g.n, rw = d.g.rw, rwp = d.g.rwp, S = d.S, npad = d.g.npad;
     const uint32_t* CR_RESTRICT nbr = d.g.nbr;
-    const uint32_t* CR_RESTRICT iso = d.g.isolated;
+    const uint32_t* CR_RESTRICT iso = cop_iso(d.g);     // cops that cannot move
     const uint8_t* CR_RESTRICT cover = d.g.cover;
     const size_t plane = (size_t)n * npad * W;          // bytes of one cover plane
     const bool aligned = (n & 7) == 0, single = n <= 256;
@@ -597,8 +597,8 @@ __device__ CR_BODY_INLINE void cop_pull_body(const V1Dev& d, int col, int nx, un
     uint32_t* wnew = wacc + S * rwp;
     const uint32_t* CR_RESTRICT fin = d.front + (size_t)nx * d.C * S * rwp;
     const uint8_t* CR_RESTRICT fflag_in = d.fflag + (size_t)nx * d.C;
-    const uint32_t* CR_RESTRICT rp = d.g.row_ptr;
-    const uint16_t* CR_RESTRICT adj = d.g.col;
+    const uint32_t* CR_RESTRICT rp = cop_rows(d.g);     // the cops' moves
+    const uint16_t* CR_RESTRICT adj = cop_cols(d.g);
     const bool vec4 = (rwp & 3) == 0;
     const bool spec = (unsigned long long)mi.rows * 2 >= d.C;   // at least half the rows flagged
     Tally t;
@@ -743,7 +743,7 @@ __device__ CR_BODY_INLINE void cop_seed_body(const V1Dev& d, int col, int nx, un
     const int append = d.meta[col].append;
     uint32_t* wacc = sm + (warp * CPW + L.grp) * (2 * S * rwp);
     uint32_t* wnew = wacc + S * rwp;
-    const uint32_t* CR_RESTRICT rp = d.g.row_ptr;
+    const uint32_t* CR_RESTRICT rp = cop_rows(d.g);     // the cops' moves
     Tally t;
     const size_t step = (size_t)nwk * (blockDim.x >> 5) * CPW;
     for (size_t cb = ((size_t)wk * (blockDim.x >> 5) + warp) * CPW; cb < d.C; cb += step) {

@@ -18,6 +18,8 @@ ERRORS = {
 }
 CR_RULES_V1 = 1
 CR_RULES_V2 = 2
+CR_COP_STAY = 0x10
+CR_ROBBER_STAY = 0x20
 CR_MAX_K = 4
 
 c_u64p = ctypes.POINTER(ctypes.c_uint64)

@@ -41,6 +41,12 @@ extern "C" {
 /* Rule sets (the two live solvers of the reference). */
 #define CR_RULES_V1 1 /* solvers/k_cops_visibility.cpp: 2p DP columns per cycle */
 #define CR_RULES_V2 2 /* solvers/k_cops_visibility_v2.cpp: one plane, macro-turn search */
+/* Flags OR-ed into CR_RULES_V1: the stay-allowed variants.  The reference's AuxGraph carries
+ * them (copSelfEdges, lib/include/AuxGraph.h:38-39, 89-90, 203-205; robberSelfEdges,
+ * solvers/k_cops_visibility.cpp:253-255) with both hard-coded off in its solvers; with both on
+ * the game is the classical one of legacy/src/k_cops_4.cpp. */
+#define CR_COP_STAY 0x10    /* a cop may stay on its vertex */
+#define CR_ROBBER_STAY 0x20 /* the robber may stay on its vertex */
 
 #define CR_MAX_K 4      /* cops per configuration handled by the device kernels */
 #define CR_MAX_N 1024   /* vertices */

@@ -117,11 +117,14 @@ def transitions(graph, k: int, cfg: np.ndarray, cop_stay: bool = False):
     return heads, data[: int(heads[-1])]
 
 
-def solve_v1(graph, k: int, p: int = 1, threads: int = 0, max_passes: int = 4096) -> Solution:
-    """v1 (solvers/k_cops_visibility.cpp) restated: the 2p-column sweep to its fixed point."""
+def solve_v1(graph, k: int, p: int = 1, threads: int = 0, max_passes: int = 4096,
+             cop_stay: bool = False, robber_stay: bool = False) -> Solution:
+    """v1 (solvers/k_cops_visibility.cpp) restated: the 2p-column sweep to its fixed point.
+    cop_stay / robber_stay: the self-edge rules of AuxGraph.h:203-205 and
+    k_cops_visibility.cpp:253-255 (off in the reference's solvers)."""
     L = lib()
     cfg = configs(graph.n, k)
-    heads, trans = transitions(graph, k, cfg)
+    heads, trans = transitions(graph, k, cfg, cop_stay)
     cols = 2 * p
     states = np.empty(cfg.shape[0] * graph.n * cols, dtype=np.uint8)
     row_ptr, col = graph.csr()
@@ -129,7 +132,7 @@ def solve_v1(graph, k: int, p: int = 1, threads: int = 0, max_passes: int = 4096
     caps = ctypes.c_uint64(0)
     counts = np.zeros(max_passes, dtype=np.uint64)
     tr = trans if trans.size else np.zeros(1, np.uint64)
-    passes = L.or_v1_solve(graph.n, _p(row_ptr, u32p), _p(col, u16p), k, p, 0, 0,
+    passes = L.or_v1_solve(graph.n, _p(row_ptr, u32p), _p(col, u16p), k, p, int(cop_stay), int(robber_stay),
                            _p(cfg, u16p), cfg.shape[0], _p(heads, u64p), _p(tr, u64p),
                            _p(states, u8p), ctypes.byref(caps), _p(counts, u64p), max_passes,
                            threads)

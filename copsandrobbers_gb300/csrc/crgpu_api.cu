@@ -21,6 +21,8 @@ void launch_and(const V1Dev& d, int col, bool p1, int grid, cudaStream_t st);
 void launch_prep(const V1Dev& d, int col, int nx, int grid, cudaStream_t st);
 void launch_init(const V1Dev& d, int grid, cudaStream_t st);
 void launch_init_pass1(const V1Dev& d, int grid, cudaStream_t st);
+void launch_marks_from_table(const uint8_t* table, uint32_t C, int n, int cols, int rwp, uint32_t* marked,
+                             int grid, cudaStream_t st);
 void launch_game(const uint8_t* table, const uint16_t* configs, const unsigned long long* heads,
                  const unsigned long long* trans, const uint32_t* rp, const uint16_t* adj, int n, int k,
                  long long best, int cap, long long* out_c, int* out_r, int* count, int* captured,
@@ -1148,6 +1150,61 @@ int cr_solver_write_table_file(cr_solver* s, const char* path) {
     ok = ok && fwrite(buf.data(), 1, states, f) == states;
     ok = (fclose(f) == 0) && ok;
     if (!ok) return fail(ctx, CR_ERR_IO, "short write to %s", path);
+    return CR_OK;
+}
+
+int cr_solver_load_table_file(cr_solver* s, const char* path) {
+    if (!s || !path) return CR_ERR_INVALID;
+    cr_context* ctx = s->ctx;
+    if (s->rules != CR_RULES_V1) return fail(ctx, CR_ERR_LIMIT, "table files load into v1 solvers");
+    if (s->n > 256) return fail(ctx, CR_ERR_LIMIT, "the table file stores vertices as uint8 (n <= 256)");
+    FILE* f = fopen(path, "rb");
+    if (!f) return fail(ctx, CR_ERR_IO, "cannot open %s", path);
+    std::vector<uint8_t> blob;
+    {
+        uint8_t buf[1 << 16];
+        size_t got;
+        while ((got = fread(buf, 1, sizeof(buf), f)) > 0) blob.insert(blob.end(), buf, buf + got);
+        fclose(f);
+    }
+    if (blob.size() < 96) return fail(ctx, CR_ERR_IO, "%s: short header", path);
+    uint64_t h[12];
+    memcpy(h, blob.data(), 96);
+    const uint64_t states = s->C * (uint64_t)s->n * s->cols;
+    // the key fields (CacheManager.h:88-104): k, N, columns, configCount, numStates, the item
+    // size and the self-edge rules
+    if (h[0] != (uint64_t)s->k || h[1] != (uint64_t)s->n || h[2] != (uint64_t)s->cols || h[3] != s->C ||
+        h[4] != states || h[5] != 1 || h[6] != (uint64_t)s->cop_stay || h[7] != (uint64_t)s->robber_stay)
+        return fail(ctx, CR_ERR_INVALID, "%s was written for another solve", path);
+    const uint64_t cfg = s->C * (uint64_t)s->k, heads = (s->C + 1) * 8;
+    if (h[8] != 96 || h[9] != 96 + cfg || h[10] != h[9] + heads || h[11] < h[10] || (h[11] - h[10]) % 8 ||
+        blob.size() != h[11] + states)
+        return fail(ctx, CR_ERR_IO, "%s: sections do not match the header", path);
+    std::vector<uint8_t> mine(cfg);
+    int rc = cr_solver_read_configs(s, mine.data(), mine.size());
+    if (rc) return rc;
+    if (memcmp(mine.data(), blob.data() + h[8], cfg) != 0)
+        return fail(ctx, CR_ERR_INVALID, "%s: configs section differs from this solver's", path);
+    CR_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    const uint64_t ntrans = (h[11] - h[10]) / 8;
+    if (!s->d_heads) CR_CUDA(ctx, cudaMalloc(&s->d_heads, heads));
+    if (s->d_trans && ntrans > s->n_trans) {
+        cudaFree(s->d_trans);
+        s->d_trans = nullptr;
+    }
+    if (!s->d_trans) CR_CUDA(ctx, cudaMalloc(&s->d_trans, std::max<uint64_t>(ntrans, 1) * 8));
+    s->n_trans = ntrans;
+    CR_CUDA(ctx, cudaMemcpyAsync(s->d_heads, blob.data() + h[9], heads, cudaMemcpyHostToDevice, st));
+    if (ntrans) CR_CUDA(ctx, cudaMemcpyAsync(s->d_trans, blob.data() + h[10], ntrans * 8, cudaMemcpyHostToDevice, st));
+    CR_CUDA(ctx, cudaMemcpyAsync(s->d_table, blob.data() + h[11], states, cudaMemcpyHostToDevice, st));
+    launch_marks_from_table(s->d_table, (uint32_t)s->C, s->n, s->cols, s->rwp, s->d_marked, ctx->num_sms * 8, st);
+    CR_CUDA(ctx, cudaGetLastError());
+    CR_CUDA(ctx, cudaStreamSynchronize(st));   // the host blob goes out of scope
+    s->init_pending = false;
+    s->initialized = true;
+    s->finished = true;
+    s->pass_counts.clear();
     return CR_OK;
 }
 

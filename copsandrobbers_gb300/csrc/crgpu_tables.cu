@@ -279,4 +279,29 @@ void launch_game(const uint8_t* table, const uint16_t* configs, const unsigned l
     k_game<<<1, 32, 0, st>>>(table, configs, heads, trans, rp, adj, n, k, best, cap, out_c, out_r, count, captured);
 }
 
+
+// Marked bit planes from table bytes (a table read from a file): word w of row (col, cid)
+// holds the marked bits of robbers 32w .. 32w+31.
+__global__ void k_marks_from_table(const uint8_t* __restrict__ table, uint32_t C, int n, int cols, int rwp,
+                                   uint32_t* __restrict__ marked) {
+    const size_t words = (size_t)cols * C * rwp;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < words; i += (size_t)gridDim.x * blockDim.x) {
+        const int w = (int)(i % rwp);
+        const size_t row = i / rwp;
+        const uint32_t cid = (uint32_t)(row % C);
+        const int col = (int)(row / C);
+        uint32_t bits = 0;
+        for (int b = 0; b < 32; ++b) {
+            const int r = w * 32 + b;
+            if (r < n && (table[((size_t)cid * n + r) * cols + col] & 1u)) bits |= 1u << b;
+        }
+        marked[i] = bits;
+    }
+}
+
+void launch_marks_from_table(const uint8_t* table, uint32_t C, int n, int cols, int rwp, uint32_t* marked,
+                             int grid, cudaStream_t st) {
+    k_marks_from_table<<<grid, 256, 0, st>>>(table, C, n, cols, rwp, marked);
+}
+
 }  // namespace crgpu

@@ -117,14 +117,20 @@ bool buildAuxGraph() {
         std::cerr << "Error: no usable CUDA device.\n";
         return 1;
     }
-    // A table file under the same key (self-edge flags 0/0 in header words 6-7,
-    // CacheManager.h:88-96) is a hit.  initializeCaptures resets every column either way, so a
-    // hit and a miss solve identically; the file only changes what is printed here.
+    cr_graph g{g_n, g_row_ptr.data(), g_col.data()};
+    if (report(cr_solver_create(g_ctx, &g, g_k, g_p, CR_GPU_RULES, &g_solver), "Unable to generate aux graph"))
+        return 1;
+    // CacheManager::loadAuxGraph (CacheManager.h:78-141): a table file under the same key whose
+    // header matches (self-edge flags 0/0 in words 6-7) is a hit.  v1 reads it into the device
+    // store; for v2 the header check alone decides.  initializeCaptures resets every column
+    // either way, so a hit and a miss solve identically.
     bool hit = false;
     if (FILE* f = std::fopen(cache_path().c_str(), "rb")) {
         uint64_t h[12];
         hit = std::fread(h, 8, 12, f) == 12 && h[6] == 0 && h[7] == 0;
         std::fclose(f);
+        if (hit && CR_GPU_RULES == CR_RULES_V1)
+            hit = cr_solver_load_table_file(g_solver, cache_path().c_str()) == CR_OK;
     }
     if (hit) {
         std::cout << "Loaded AuxGraph from cache!\n";
@@ -133,9 +139,6 @@ bool buildAuxGraph() {
     } else {
         std::cout << "Cache miss. Creating new AuxGraph with " << g_columns << " columns...\n";
     }
-    cr_graph g{g_n, g_row_ptr.data(), g_col.data()};
-    if (report(cr_solver_create(g_ctx, &g, g_k, g_p, CR_GPU_RULES, &g_solver), "Unable to generate aux graph"))
-        return 1;
     if (!hit) {
         cr_table_sizes sz;
         cr_solver_sizes(g_solver, &sz);

@@ -116,6 +116,7 @@ SIGNATURES = {
                                       ctypes.c_int32, ctypes.c_int32, c_i32p, ctypes.POINTER(CrBatchResult),
                                       ctypes.POINTER(CrBatchStats)]),
     "cr_solver_digest": (ctypes.c_int, [ctypes.c_void_p, c_u64p]),
+    "cr_solver_load_table_file": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
     "cr_solver_perfect_game": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64),
                                               ctypes.POINTER(ctypes.c_int32), ctypes.c_int32,
                                               ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),

@@ -171,6 +171,10 @@ class Solver:
     def write_table_file(self, path: str) -> None:
         _check(self.ctx.ptr, N.lib().cr_solver_write_table_file(self.ptr, path.encode()))
 
+    def load_table_file(self, path: str) -> None:
+        """A table file of this solve back into the device store (a solved table)."""
+        _check(self.ctx.ptr, N.lib().cr_solver_load_table_file(self.ptr, path.encode()))
+
     def close(self) -> None:
         if self.ptr:
             N.lib().cr_solver_destroy(self.ptr)

@@ -147,6 +147,15 @@ int cr_solver_read_transitions(cr_solver* s, uint64_t* heads, size_t heads_len,
 /* outputData (k_cops_visibility.cpp:356-373; CacheManager::saveAuxGraph, CacheManager.h:28-75):
  * write the whole table file (96-byte header, configs, heads, transitions, states). */
 int cr_solver_write_table_file(cr_solver* s, const char* path);
+/* CacheManager::loadAuxGraph (CacheManager.h:78-141) into the device store (v1 rules): a table
+ * file whose header matches this solver (k, n, columns, configs, states, self-edge flags) is
+ * read back; its states section becomes the table, its heads and transitions sections the
+ * successor CSR, its configs section is checked against the solver's own, and the marked
+ * planes are rebuilt from the table bytes.  The loaded table answers cr_solver_verdict, the
+ * reads and cr_solver_perfect_game as a solved one; cr_solver_init then resets every column,
+ * as initializeCaptures does after a cache hit in the reference.  CR_ERR_IO when the file is
+ * missing or short, CR_ERR_INVALID when it was written for another solve. */
+int cr_solver_load_table_file(cr_solver* s, const char* path);
 
 /* ---- whole solves ---------------------------------------------------------------------- */
 

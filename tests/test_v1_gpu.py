@@ -91,3 +91,31 @@ def test_v1_table_file_bytes(gpu_ctx, tmp_path):
             path = str(tmp_path / "t.bin")
             s.write_table_file(path)
         assert hashlib.sha256(open(path, "rb").read()).hexdigest() == case["sha_file"], case_id(case)
+
+
+def test_table_file_round_trip(gpu_ctx, tmp_path):
+    """CacheManager::loadAuxGraph: a written table file loads back into a fresh solver as a
+    solved table (same bytes, verdict and perfect game); initializeCaptures then resets it."""
+    import hashlib
+    from copsandrobbers_gb300.solver import Solver
+    for case in [c for c in V1 if c["graph"] in ("peterson", "grid9", "dodecahedron") and c["p"] <= 2]:
+        g = G.load_matrix(matrix_path(case))
+        path = str(tmp_path / "t.bin")
+        with Solver(gpu_ctx, g, case["k"], case["p"]) as s:
+            s.init(); counts = s.run()
+            s.write_table_file(path)
+            st, v = s.states(), s.verdict()
+            game = s.perfect_game() if case["p"] == 1 else None
+        with Solver(gpu_ctx, g, case["k"], case["p"]) as t:
+            t.load_table_file(path)
+            assert np.array_equal(t.states(), st) and t.verdict() == v, case_id(case)
+            if game is not None:
+                assert t.perfect_game() == game
+            assert hashlib.sha256(open(path, "rb").read()).hexdigest() == case["sha_file"]
+            t.init(); assert t.run() == counts
+            assert np.array_equal(t.states(), st)
+        # written for another solve: refused
+        with Solver(gpu_ctx, g, case["k"] % 3 + 1, case["p"]) as u:
+            with pytest.raises(N.CrGpuError) as e:
+                u.load_table_file(path)
+            assert e.value.code in (1, 7)

@@ -105,6 +105,10 @@ struct cr_solver {
     // set between cr_solver_init and that pass, and undone by materialize_init() when the
     // post-initializeCaptures state is read first
     bool init_pending = false;
+    // small solves launch each pass's kernels directly: capturing and instantiating a graph
+    // costs more than it saves over a handful of short passes, and contends for the driver
+    // when many solves run side by side (the solve server)
+    bool small = false;
     uint64_t base_caps = 0;
     std::vector<uint64_t> pass_counts;
     cr_solve_stats stats{};
@@ -464,6 +468,7 @@ int cr_solver_create(cr_context* ctx, const cr_graph* g, int32_t k, int32_t p, i
     s->robber_stay = (stay & CR_ROBBER_STAY) != 0;
     s->S = slots_for(g->n);
     layout(s->n, k, p, rules, s->S, &s->C, &s->cols, &s->rw, &s->rwp);
+    s->small = s->C * (uint64_t)s->n * s->cols < (1ull << 24);
     if (s->C == 0 || s->C >= (1ull << 32)) {
         delete s;
         return fail(ctx, CR_ERR_LIMIT, "config count C(%d,%d) outside 1..2^32-1", g->n + k - 1, k);
@@ -677,8 +682,8 @@ static int v1_enqueue_pass(cr_solver* s, bool profile, bool readback = true) {
 static int v1_pass(cr_solver* s, uint64_t* found) {
     cr_context* ctx = s->ctx;
     cudaStream_t st = ctx->stream;
-    if (ctx->profiling) {
-        int rc = v1_enqueue_pass(s, true);
+    if (ctx->profiling || s->small) {
+        int rc = v1_enqueue_pass(s, ctx->profiling);
         if (rc) return rc;
     } else {
         if (!s->pass_graph) {
@@ -892,7 +897,7 @@ static int v1_run_on_device(cr_solver* s) {
 
 int cr_solver_run(cr_solver* s, uint64_t* pass_counts, int32_t cap, int32_t* passes) {
     if (!s) return CR_ERR_INVALID;
-    if (s->initialized && !s->finished && s->rules == CR_RULES_V1 && !s->ctx->profiling) {
+    if (s->initialized && !s->finished && s->rules == CR_RULES_V1 && !s->ctx->profiling && !s->small) {
         CR_CUDA(s->ctx, cudaSetDevice(s->ctx->device));
         if (s->init_pending) {
             uint64_t f;

@@ -25,7 +25,8 @@ EXE = os.path.join(BIN, "k_cops_gpu")
 
 CU_SOURCES = ["crgpu_api.cu", "crgpu_v1.cu", "crgpu_v2.cu", "crgpu_tables.cu", "crgpu_batch.cu",
               "crgpu_noalloc.cu", "crgpu_server.cu"]
-HEADERS = ["crgpu_internal.cuh", "crgpu_v2.h", "crgpu_batch.h", os.path.join("..", "..", "include", "crgpu.h")]
+HEADERS = ["crgpu_internal.cuh", "crgpu_v1_body.cuh", "crgpu_ctx.h", "crgpu_v2.h", "crgpu_batch.h",
+           os.path.join("..", "..", "include", "crgpu.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -373,26 +373,30 @@ __device__ CR_BODY_INLINE void init_pass1_body(const V1Dev& d, unsigned wk, unsi
                 const uint32_t deepb = ~zn.zero_bits();
                 a2 = a & deepb;
                 a1 = a & ~deepb;
-                // bytes: column 0 = 0x01 cop / 0x03 seed / 0xFE; column 1 = 0x01 cop / 0x03
-                // round 1 / 0x05 round 2 / 0xFE (0xFE ^ 0xFF, ^ 0xFD, ^ 0xFB); state (r, col) is
-                // byte 2r + col of the row
-                uint32_t q[4];
-#pragma unroll
-                for (int g = 0; g < 2; ++g) {
-                    const uint32_t mc = nibble_bytes((capb >> (4 * g)) & 0xFu);
-                    const uint32_t ms = nibble_bytes((seedb >> (4 * g)) & 0xFu);
-                    const uint32_t m1 = nibble_bytes((a1 >> (4 * g)) & 0xFu);
-                    const uint32_t m2 = nibble_bytes((a2 >> (4 * g)) & 0xFu);
-                    const uint32_t c0 = 0xFEFEFEFEu ^ mc ^ (ms & 0xFDFDFDFDu);
-                    const uint32_t c1 = 0xFEFEFEFEu ^ mc ^ (m1 & 0xFDFDFDFDu) ^ (m2 & 0xFBFBFBFBu);
-                    q[2 * g] = __byte_perm(c0, c1, 0x5140);
-                    q[2 * g + 1] = __byte_perm(c0, c1, 0x7362);
-                }
+                // the piece: column 0 = 0x03 on the seeds (0xFE ^ 0xFD), else 0xFE; column 1 =
+                // 0xFE; state (r, col) is byte 2r + col of the row.  The few cops and column-1
+                // marks get their two bytes rewritten after the piece, in this thread's order.
                 uint8_t* dst = trow + r0 * 2;
+                const uint32_t s0 = 0xFEFEFEFEu ^ (nibble_bytes(seedb & 0xFu) & 0xFDFDFDFDu);
+                const uint32_t s1 = 0xFEFEFEFEu ^ (nibble_bytes(seedb >> 4) & 0xFDFDFDFDu);
+                const uint32_t fe = 0xFEFEFEFEu;
                 if (aligned) {
-                    *reinterpret_cast<uint4*>(dst) = make_uint4(q[0], q[1], q[2], q[3]);
+                    *reinterpret_cast<uint4*>(dst) = make_uint4(__byte_perm(s0, fe, 0x5140), __byte_perm(s0, fe, 0x7362),
+                                                                __byte_perm(s1, fe, 0x5140), __byte_perm(s1, fe, 0x7362));
                 } else {
-                    for (int b = 0; b < 16 && r0 + (b >> 1) < n; ++b) dst[b] = (uint8_t)(q[b >> 2] >> ((b & 3) * 8));
+                    for (int b = 0; b < 16 && r0 + (b >> 1) < n; ++b)
+                        dst[b] = (b & 1) ? 0xFE : (((seedb >> (b >> 1)) & 1u) ? 0x03 : 0xFE);
+                }
+                uint32_t special = capb | a1 | a2;
+                while (special) {
+                    const int j = __ffs(special) - 1;
+                    special &= special - 1;
+                    const uint32_t bit = 1u << j;
+                    // column 0: 0x01 cop / 0x03 seed / 0xFE; column 1: 0x01 cop / 0x03 round 1 /
+                    // 0x05 round 2 / 0xFE
+                    const uint32_t v0 = (capb & bit) ? 0x01u : ((seedb & bit) ? 0x03u : 0xFEu);
+                    const uint32_t v1 = (capb & bit) ? 0x01u : ((a1 & bit) ? 0x03u : ((a2 & bit) ? 0x05u : 0xFEu));
+                    *reinterpret_cast<uint16_t*>(dst + 2 * j) = (uint16_t)(v0 | (v1 << 8));
                 }
                 cnt += __popc(seedb) + __popc(a1) + __popc(a2);
                 any_seed |= seedb;
@@ -408,13 +412,21 @@ __device__ CR_BODY_INLINE void init_pass1_body(const V1Dev& d, unsigned wk, unsi
             const uint32_t t01 = __byte_perm(v, v1, 0x5140), t01b = __byte_perm(v, v1, 0x7362);
             const uint32_t t23 = __byte_perm(v2, v3, 0x5140), t23b = __byte_perm(v2, v3, 0x7362);
             const int w = it * 8 + (lane >> 2);
-            if ((lane & 3) == 0 && w < rw) {
+            const bool writer = (lane & 3) == 0 && w < rw;
+            if (writer) {
                 m0row[w] = __byte_perm(t01, t23, 0x5410);
                 m1row[w] = __byte_perm(t01, t23, 0x7632);
-                frow[w] = __byte_perm(t01b, t23b, 0x5410);
-                frow[rwp + w] = __byte_perm(t01b, t23b, 0x7632);
             }
-            changed |= (a1 | a2) != 0u;
+            // the frontier row is read only under its flag: a one-block row is written only
+            // when it changed (longer rows always, as a later block may set the flag)
+            const bool marks = __any_sync(FULL_MASK, (a1 | a2) != 0u);
+            changed |= marks;
+            if (marks || !single) {
+                if (writer) {
+                    frow[w] = __byte_perm(t01b, t23b, 0x5410);
+                    frow[rwp + w] = __byte_perm(t01b, t23b, 0x7632);
+                }
+            }
         }
         if (padded) {
             for (int e = rw + lane; e < rwp; e += 32) {
@@ -425,7 +437,6 @@ __device__ CR_BODY_INLINE void init_pass1_body(const V1Dev& d, unsigned wk, unsi
             }
             for (int e = 2 * rwp + lane; e < frow_words; e += 32) frow[e] = 0u;
         }
-        changed = __any_sync(FULL_MASK, changed);
         if (lane == 0) {
             *fl0 = 1;
             *fl1 = changed ? 1 : 0;

@@ -978,6 +978,18 @@ int cr_solver_stats(cr_solver* s, cr_solve_stats* out) {
     return CR_OK;
 }
 
+int cr_solver_v2_hash_stats(cr_solver* s, cr_v2_hash_stats* out) {
+    if (!s || !out) return CR_ERR_INVALID;
+    *out = s->v2 ? crgpu::v2_hash_stats(s->v2) : cr_v2_hash_stats{};
+    return CR_OK;
+}
+
+int cr_solver_set_v2_hash_capacity(cr_solver* s, uint64_t slots) {
+    if (!s) return CR_ERR_INVALID;
+    if (!s->v2) return CR_OK;   // v1 rules: no cloud table
+    return crgpu::v2_set_hash_capacity(s->v2, slots, &s->ctx->err);
+}
+
 static const uint8_t* table_ptr(const cr_solver* s) {
     return s->rules == CR_RULES_V1 ? s->d_table : crgpu::v2_table(s->v2);
 }

@@ -21,6 +21,23 @@
 // the first pass val1 is recomputed only for configs within p-1 cop steps of a config that
 // gained marks ("dirty"); the others keep last pass's value, which is exact because the
 // snapshot they read has not changed there.
+//
+// For p >= 3 the depth-2 nodes (C2, V2) repeat heavily: V2 = N(N(r) \ C1 \ C2) \ C2 is the same
+// cloud for every predecessor C1 of C2 that misses N(r), so many depth-1 nodes share each
+// depth-2 subtree (on a Delaunay graph of 199 vertices with k = 2, one full pass visits 79.3 M
+// depth-2 children but only 4.69 M distinct ones).  Each pass therefore dedups the reachable
+// depth-2 clouds in a device hash table before any leaf is read:
+//   k_v2_hinsert  every dirty depth-1 node inserts its non-terminal children (C2, V2): key =
+//                 (rank of C2 + 1) << 32 | 32-bit fingerprint of V2, claimed by atomicCAS with
+//                 linear probing; the claiming thread writes the full cloud beside the key;
+//   k_v2_heval    one thread per occupied slot takes the exact subtree minimum of its node;
+//   k_v2_val1     looks every child up (key equal AND full cloud equal) and takes the stored
+//                 value; a child it does not find (probe limit, table full, or a fingerprint
+//                 shared by two clouds of the same C2, whose second cloud never got a slot) is
+//                 evaluated directly, so the result is exact whatever the table holds.
+// The subtree value of a node depends only on (depth, C2, V2) and the pass's snapshot, so the
+// table is rebuilt every pass.  When the depth-1 nodes outnumber half the table, they are
+// processed in chunks, each with a fresh table.
 #include <algorithm>
 #include <string>
 #include <vector>
@@ -56,6 +73,13 @@ struct V2Solver {
     unsigned long long* counters = nullptr;
     unsigned int* err = nullptr;
     unsigned long long* h_pinned = nullptr;
+    // depth-2 cloud table (p >= 3): keys, clouds [hcap][rwp] and subtree values
+    unsigned long long* hkey = nullptr;
+    uint32_t* hmask = nullptr;
+    uint8_t* hval = nullptr;
+    uint64_t hcap = 0;
+    uint64_t chunk_nodes = 0;   // depth-1 nodes per table fill
+    cr_v2_hash_stats hstats{};
     bool first = true;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
 };
@@ -73,8 +97,15 @@ struct V2Dev {
     uint8_t* val1;
     uint8_t* newval;
     const uint8_t* dirty;
-    unsigned long long* count;
+    unsigned long long* count;     // [0] marks found, [1] depth-2 child visits, [2] table entries
+    unsigned long long* hkey;      // null = no cloud table (p < 3)
+    uint32_t* hmask;
+    uint8_t* hval;
+    uint64_t hcap;                 // power of two
+    uint64_t node_lo, node_hi;     // depth-1 nodes (C1 * n + r) of this chunk
 };
+
+constexpr int kHashProbes = 64;   // linear-probe limit of an insert or a lookup
 
 template <int W>
 struct Mask {
@@ -244,30 +275,193 @@ __device__ int subtree_min(const V2Dev& d, const int (&c2)[K], const Mask<W>& V2
     return best;
 }
 
+// Minimum over the children of depth-2 node (c2, V2) when p = 3 (the children are leaves):
+// cop ply 3 empties the cloud -> 5, robber ply 3 leaves nobody -> 6, else the leaf cost.
+template <int W, int K>
+__device__ int node2_min_p3(const V2Dev& d, const int (&c2)[K], const Mask<W>& V2, const uint32_t* snbr) {
+    Moves<K> mv;
+    moves_of<K>(mv, c2, d.rp);
+    const Mask<W> E = expand<W>(V2, snbr, d.rwp);
+    const int np1 = d.n + 1;
+    int best = kV2None;
+    for (int t = 0; t < mv.T; ++t) {
+        int c[K];
+        const uint32_t cid = move_target<K>(mv, t, d.col, d.binom, np1, c);
+        Mask<W> nx;
+        if (mask_hits<W, K>(V2, c)) {
+            Mask<W> mid = V2;
+            mask_clear<W, K>(mid, c);
+            if (mask_empty<W>(mid)) return 5;   // the smallest value a depth-2 node can take
+            nx = expand<W>(mid, snbr, d.rwp);
+        } else {
+            nx = E;
+        }
+        mask_clear<W, K>(nx, c);
+        if (mask_empty<W>(nx)) { best = 6; continue; }
+        if (best > 6) best = min(best, leaf_cost<W>(d, cid, nx));
+    }
+    return best;
+}
+
+// Cloud-table key of depth-2 node (cid, V): the config's rank + 1 above a 32-bit fingerprint
+// of the cloud (never 0, which marks an empty slot).
+template <int W>
+__device__ __forceinline__ unsigned long long cloud_key(uint32_t cid, const Mask<W>& V) {
+    uint32_t h = 0x9E3779B9u;
+#pragma unroll
+    for (int j = 0; j < W; ++j) {
+        h = (h ^ V.w[j]) * 0x85EBCA6Bu;
+        h ^= h >> 13;
+    }
+    h *= 0xC2B2AE35u;
+    h ^= h >> 16;
+    return ((unsigned long long)(cid + 1u) << 32) | h;
+}
+
+__device__ __forceinline__ uint64_t cloud_slot(unsigned long long key, uint64_t cap) {
+    uint64_t z = key + 0x9E3779B97F4A7C15ull;   // splitmix64 finaliser
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return (z ^ (z >> 31)) & (cap - 1);
+}
+
+// Insert (cid, V) unless its key is present; the thread that claims a slot writes the cloud.
+// Returns 1 when this call claimed a new slot.
+template <int W>
+__device__ __forceinline__ unsigned cloud_insert(const V2Dev& d, uint32_t cid, const Mask<W>& V) {
+    const unsigned long long key = cloud_key<W>(cid, V);
+    uint64_t h = cloud_slot(key, d.hcap);
+    for (int probe = 0; probe < kHashProbes; ++probe) {
+        const unsigned long long old = atomicCAS(&d.hkey[h], 0ull, key);
+        if (old == 0ull) {
+            uint32_t* m = d.hmask + h * d.rwp;
+#pragma unroll
+            for (int j = 0; j < W; ++j)
+                if (j < d.rwp) m[j] = V.w[j];
+            return 1u;
+        }
+        if (old == key) return 0u;
+        h = (h + 1) & (d.hcap - 1);
+    }
+    return 0u;   // probe limit: the lookup misses and the node is evaluated directly
+}
+
+// Stored value of (cid, V), or -1 when the table does not hold exactly this node.
+template <int W>
+__device__ __forceinline__ int cloud_lookup(const V2Dev& d, uint32_t cid, const Mask<W>& V) {
+    const unsigned long long key = cloud_key<W>(cid, V);
+    uint64_t h = cloud_slot(key, d.hcap);
+    for (int probe = 0; probe < kHashProbes; ++probe) {
+        const unsigned long long k = __ldg(&d.hkey[h]);
+        if (k == 0ull) return -1;
+        if (k == key) {
+            const uint32_t* m = d.hmask + h * d.rwp;
+            bool same = true;
+#pragma unroll
+            for (int j = 0; j < W; ++j)
+                if (j < d.rwp) same &= __ldg(&m[j]) == V.w[j];
+            return same ? (int)__ldg(&d.hval[h]) : -1;
+        }
+        h = (h + 1) & (d.hcap - 1);
+    }
+    return -1;
+}
+
+// Depth-1 node (c1, r) of a chunk: its cops and cloud N(r) \ C1; false when the node is
+// decided without children (r on a cop, or no robber move left).
+template <int W, int K>
+__device__ __forceinline__ bool depth1_node(const V2Dev& d, uint32_t c1, int r, const uint32_t* snbr,
+                                            int (&cops1)[K], Mask<W>& V1) {
+    bool rin = false;
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+        cops1[i] = d.configs[(size_t)c1 * K + i];
+        rin |= cops1[i] == r;
+    }
+    load_nbr<W>(V1, snbr, d.rwp, r);
+    mask_clear<W, K>(V1, cops1);
+    return !(rin || mask_empty<W>(V1));
+}
+
+// Fill the cloud table with the distinct non-terminal depth-2 children of the chunk's dirty
+// depth-1 nodes: a warp per node, lanes over the cop moves.
+template <int K, int W>
+__global__ void __launch_bounds__(256) k_v2_hinsert(V2Dev d) {
+    extern __shared__ uint32_t snbr[];
+    for (int i = threadIdx.x; i < d.n * d.rwp; i += blockDim.x) snbr[i] = d.nbr[i];
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const size_t nwarps = (size_t)gridDim.x * (blockDim.x >> 5);
+    const int np1 = d.n + 1;
+    unsigned visits = 0, fresh = 0;
+    for (size_t idx = d.node_lo + (size_t)blockIdx.x * (blockDim.x >> 5) + warp; idx < d.node_hi; idx += nwarps) {
+        const uint32_t c1 = (uint32_t)(idx / d.n);
+        const int r = (int)(idx - (size_t)c1 * d.n);
+        if (!d.dirty[c1]) continue;
+        int cops1[K];
+        Mask<W> V1;
+        if (!depth1_node<W, K>(d, c1, r, snbr, cops1, V1)) continue;
+        Moves<K> mv;
+        moves_of<K>(mv, cops1, d.rp);
+        for (int t = lane; t < mv.T; t += 32) {
+            int c2[K];
+            const uint32_t cid2 = move_target<K>(mv, t, d.col, d.binom, np1, c2);
+            if (cid2 >= d.C) continue;
+            Mask<W> mid = V1;
+            mask_clear<W, K>(mid, c2);
+            if (mask_empty<W>(mid)) continue;
+            Mask<W> nx = expand<W>(mid, snbr, d.rwp);
+            mask_clear<W, K>(nx, c2);
+            if (mask_empty<W>(nx)) continue;
+            ++visits;
+            fresh += cloud_insert<W>(d, cid2, nx);
+        }
+    }
+    visits = __reduce_add_sync(0xFFFFFFFFu, visits);
+    fresh = __reduce_add_sync(0xFFFFFFFFu, fresh);
+    if (lane == 0) {
+        if (visits) atomicAdd(&d.count[1], (unsigned long long)visits);
+        if (fresh) atomicAdd(&d.count[2], (unsigned long long)fresh);
+    }
+}
+
+// Exact subtree minimum of every node in the cloud table: a thread per slot.
+template <int K, int W>
+__global__ void __launch_bounds__(256) k_v2_heval(V2Dev d) {
+    extern __shared__ uint32_t snbr[];
+    for (int i = threadIdx.x; i < d.n * d.rwp; i += blockDim.x) snbr[i] = d.nbr[i];
+    __syncthreads();
+    for (uint64_t h = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; h < d.hcap;
+         h += (uint64_t)gridDim.x * blockDim.x) {
+        const unsigned long long key = d.hkey[h];
+        if (key == 0ull) continue;
+        const uint32_t cid = (uint32_t)(key >> 32) - 1u;
+        int c2[K];
+#pragma unroll
+        for (int i = 0; i < K; ++i) c2[i] = d.configs[(size_t)cid * K + i];
+        Mask<W> V;
+#pragma unroll
+        for (int j = 0; j < W; ++j) V.w[j] = j < d.rwp ? d.hmask[h * d.rwp + j] : 0u;
+        const int v = d.p == 3 ? node2_min_p3<W, K>(d, c2, V, snbr) : subtree_min<W, K>(d, c2, V, snbr, kV2None);
+        d.hval[h] = (uint8_t)min(v, kV2None);
+    }
+}
+
 template <int K, int W>
 __global__ void __launch_bounds__(256) k_v2_val1(V2Dev d) {
     extern __shared__ uint32_t snbr[];
     for (int i = threadIdx.x; i < d.n * d.rwp; i += blockDim.x) snbr[i] = d.nbr[i];
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const size_t total = (size_t)d.C * d.n;
     const size_t nwarps = (size_t)gridDim.x * (blockDim.x >> 5);
     const int np1 = d.n + 1;
-    for (size_t idx = (size_t)blockIdx.x * (blockDim.x >> 5) + warp; idx < total; idx += nwarps) {
+    for (size_t idx = d.node_lo + (size_t)blockIdx.x * (blockDim.x >> 5) + warp; idx < d.node_hi; idx += nwarps) {
         const uint32_t c1 = (uint32_t)(idx / d.n);
         const int r = (int)(idx - (size_t)c1 * d.n);
         if (!d.dirty[c1]) continue;
         int cops1[K];
-        bool rin = false;
-#pragma unroll
-        for (int i = 0; i < K; ++i) {
-            cops1[i] = d.configs[(size_t)c1 * K + i];
-            rin |= cops1[i] == r;
-        }
         Mask<W> V1;
-        load_nbr<W>(V1, snbr, d.rwp, r);
-        mask_clear<W, K>(V1, cops1);
-        if (rin || mask_empty<W>(V1)) {
+        if (!depth1_node<W, K>(d, c1, r, snbr, cops1, V1)) {
             if (lane == 0) d.val1[idx] = kV2None;
             continue;
         }
@@ -287,7 +481,11 @@ __global__ void __launch_bounds__(256) k_v2_val1(V2Dev d) {
                 mask_clear<W, K>(nx, c2);
                 if (mask_empty<W>(nx)) { best = min(best, 4); continue; }
                 if (d.p == 2) best = min(best, leaf_cost<W>(d, cid2, nx));
-                else if (best > 5) best = subtree_min<W, K>(d, c2, nx, snbr, best);
+                else if (best > 5) {
+                    // the cloud table holds the node unless an insert gave up on it
+                    const int v = d.hkey ? cloud_lookup<W>(d, cid2, nx) : -1;
+                    best = v >= 0 ? min(best, v) : subtree_min<W, K>(d, c2, nx, snbr, best);
+                }
             }
         }
         best = __reduce_min_sync(0xFFFFFFFFu, best);
@@ -402,14 +600,23 @@ __global__ void k_v2_dilate(const uint8_t* __restrict__ in, uint8_t* out, const 
 
 // ------------------------------------------------------------------------------ host ---
 
+// Slots of the depth-2 cloud table: twice the depth-1 nodes (about 1.2 distinct children per
+// node on the graphs measured), a power of two between 2^10 and 2^24; 0 below p = 3.
+static uint64_t v2_hash_capacity(uint64_t nodes, int p) {
+    if (p < 3) return 0;
+    uint64_t cap = 1024;
+    while (cap < 2 * nodes && cap < (1ull << 24)) cap <<= 1;
+    return cap;
+}
+
 uint64_t v2_footprint(int n, int k, int p) {
-    (void)p;
     long double C = 1;
     for (int i = 1; i <= k; ++i) C = C * (n + k - i) / i;
     const uint64_t c = (uint64_t)C;
     const int rwp = round_words((n + 31) / 32);
+    const uint64_t hcap = v2_hash_capacity(c * (uint64_t)n, p);
     return c * n * 3 + c * (uint64_t)rwp * 4 + c * 3 + (uint64_t)n * rwp * 4 + c * (uint64_t)k * 2 +
-           (1u << 16);
+           hcap * (8 + 4 * (uint64_t)rwp + 1) + (1u << 16);
 }
 
 static int v2_w(int rwp) { return rwp <= 1 ? 1 : rwp <= 2 ? 2 : rwp <= 4 ? 4 : rwp <= 8 ? 8 : 16; }
@@ -420,6 +627,9 @@ static V2Dev v2_view(const V2Solver* s) {
     d.rp = s->rp; d.col = s->col; d.binom = s->binom; d.configs = s->configs;
     d.table = s->table; d.marked = s->marked; d.nbr = s->nbr;
     d.val1 = s->val1; d.newval = s->newval; d.dirty = s->dirty; d.count = s->counters;
+    d.hkey = s->hkey; d.hmask = s->hmask; d.hval = s->hval; d.hcap = s->hcap;
+    d.node_lo = 0;
+    d.node_hi = (uint64_t)s->C * s->n;
     return d;
 }
 
@@ -431,6 +641,35 @@ static V2Dev v2_view(const V2Solver* s) {
             return e_ == cudaErrorMemoryAllocation ? CR_ERR_NOMEM : CR_ERR_CUDA;          \
         }                                                                                 \
     } while (0)
+
+int v2_set_hash_capacity(V2Solver* s, uint64_t slots, std::string* err) {
+    if (s->p < 3) slots = 0;
+    uint64_t cap = 0;
+    if (slots) {
+        if (slots > (1ull << 40)) {
+            if (err) *err = "v2 cloud table: at most 2^40 slots";
+            return CR_ERR_LIMIT;
+        }
+        cap = 1024;
+        while (cap < slots) cap <<= 1;
+    }
+    V2_CUDA(cudaStreamSynchronize(s->st));
+    void* old[] = {s->hkey, s->hmask, s->hval};
+    for (void* q : old)
+        if (q) cudaFree(q);
+    s->hkey = nullptr;
+    s->hmask = nullptr;
+    s->hval = nullptr;
+    s->hcap = cap;
+    s->chunk_nodes = cap / 2;
+    s->hstats.capacity = cap;
+    if (cap) {
+        V2_CUDA(cudaMalloc(&s->hkey, cap * sizeof(unsigned long long)));
+        V2_CUDA(cudaMalloc(&s->hmask, cap * s->rwp * sizeof(uint32_t)));
+        V2_CUDA(cudaMalloc(&s->hval, cap));
+    }
+    return CR_OK;
+}
 
 int v2_create(V2Solver** out, cudaStream_t st, int num_sms, int n, int k, int p,
               const uint32_t* d_rp, const uint16_t* d_col, const uint32_t* h_rp,
@@ -460,6 +699,7 @@ int v2_create(V2Solver** out, cudaStream_t st, int num_sms, int n, int k, int p,
     V2_CUDA(cudaMalloc(&s->dirty, C));
     V2_CUDA(cudaMalloc(&s->tmp, C));
     V2_CUDA(cudaMalloc(&s->counters, 4 * sizeof(unsigned long long)));
+    if (int rc = v2_set_hash_capacity(s, v2_hash_capacity((uint64_t)C * n, p), err)) return rc;
     V2_CUDA(cudaMallocHost(&s->h_pinned, 4 * sizeof(unsigned long long)));
     V2_CUDA(cudaEventCreate(&s->e0));
     V2_CUDA(cudaEventCreate(&s->e1));
@@ -473,7 +713,8 @@ int v2_create(V2Solver** out, cudaStream_t st, int num_sms, int n, int k, int p,
 
 void v2_destroy(V2Solver* s) {
     if (!s) return;
-    void* ptrs[] = {s->table, s->marked, s->nbr, s->val1, s->newval, s->changed, s->dirty, s->tmp, s->counters};
+    void* ptrs[] = {s->table, s->marked, s->nbr, s->val1, s->newval, s->changed, s->dirty, s->tmp, s->counters,
+                    s->hkey, s->hmask, s->hval};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     if (s->h_pinned) cudaFreeHost(s->h_pinned);
@@ -503,25 +744,54 @@ int v2_init(V2Solver* s, uint64_t* caps, cr_solve_stats* stats, std::string* err
     stats->init_ms = ms;
     stats->kernel_launches = 1;
     s->first = true;
+    s->hstats = cr_v2_hash_stats{};
+    s->hstats.capacity = s->hcap;
     return CR_OK;
 }
 
+// Depth-1 values of the nodes [lo, hi): with a cloud table, fill it and evaluate its nodes
+// first.  Returns the kernels launched.
 template <int K, int W>
-static void launch_v2_kernels(const V2Dev& d, int grid_pairs, int grid_cfg, size_t sm, cudaStream_t st) {
+static int launch_v2_val1(V2Solver* s, V2Dev d, uint64_t lo, uint64_t hi, int grid_pairs, size_t sm) {
+    cudaStream_t st = s->st;
     cudaFuncSetAttribute(k_v2_val1<K, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    cudaFuncSetAttribute(k_v2_root<K, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    d.node_lo = lo;
+    d.node_hi = hi;
+    int launches = 0;
+    if (d.hkey) {
+        cudaFuncSetAttribute(k_v2_hinsert<K, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaFuncSetAttribute(k_v2_heval<K, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaMemsetAsync(d.hkey, 0, d.hcap * sizeof(unsigned long long), st);
+        k_v2_hinsert<K, W><<<grid_pairs, 256, sm, st>>>(d);
+        const int grid_h = (int)std::max<uint64_t>(1, std::min<uint64_t>((d.hcap + 255) / 256, (uint64_t)s->num_sms * 8));
+        k_v2_heval<K, W><<<grid_h, 256, sm, st>>>(d);
+        launches += 2;
+        ++s->hstats.fills;
+    }
     k_v2_val1<K, W><<<grid_pairs, 256, sm, st>>>(d);
-    k_v2_root<K, W><<<grid_cfg, 256, sm, st>>>(d);
+    return launches + 1;
+}
+
+template <int K, int W>
+static int launch_v2_kernels(V2Solver* s, const V2Dev& d, int grid_pairs, int grid_cfg, size_t sm) {
+    int launches = 0;
+    const uint64_t nodes = (uint64_t)s->C * s->n;
+    const uint64_t chunk = d.hkey ? std::max<uint64_t>(1, s->chunk_nodes) : nodes;
+    for (uint64_t lo = 0; lo < nodes; lo += chunk)
+        launches += launch_v2_val1<K, W>(s, d, lo, std::min(nodes, lo + chunk), grid_pairs, sm);
+    cudaFuncSetAttribute(k_v2_root<K, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_v2_root<K, W><<<grid_cfg, 256, sm, s->st>>>(d);
+    return launches + 1;
 }
 
 template <int K>
-static void launch_v2_k(const V2Dev& d, int W, int grid_pairs, int grid_cfg, size_t sm, cudaStream_t st) {
+static int launch_v2_k(V2Solver* s, const V2Dev& d, int W, int grid_pairs, int grid_cfg, size_t sm) {
     switch (W) {
-        case 1: launch_v2_kernels<K, 1>(d, grid_pairs, grid_cfg, sm, st); break;
-        case 2: launch_v2_kernels<K, 2>(d, grid_pairs, grid_cfg, sm, st); break;
-        case 4: launch_v2_kernels<K, 4>(d, grid_pairs, grid_cfg, sm, st); break;
-        case 8: launch_v2_kernels<K, 8>(d, grid_pairs, grid_cfg, sm, st); break;
-        default: launch_v2_kernels<K, 16>(d, grid_pairs, grid_cfg, sm, st); break;
+        case 1: return launch_v2_kernels<K, 1>(s, d, grid_pairs, grid_cfg, sm);
+        case 2: return launch_v2_kernels<K, 2>(s, d, grid_pairs, grid_cfg, sm);
+        case 4: return launch_v2_kernels<K, 4>(s, d, grid_pairs, grid_cfg, sm);
+        case 8: return launch_v2_kernels<K, 8>(s, d, grid_pairs, grid_cfg, sm);
+        default: return launch_v2_kernels<K, 16>(s, d, grid_pairs, grid_cfg, sm);
     }
 }
 
@@ -533,7 +803,7 @@ static void launch_dilate(const V2Solver* s, const uint8_t* in, uint8_t* out, in
 int v2_pass(V2Solver* s, uint64_t* found, cr_solve_stats* stats, std::string* err) {
     cudaStream_t st = s->st;
     V2_CUDA(cudaEventRecord(s->e0, st));
-    V2_CUDA(cudaMemsetAsync(s->counters, 0, sizeof(unsigned long long), st));
+    V2_CUDA(cudaMemsetAsync(s->counters, 0, 3 * sizeof(unsigned long long), st));
     const int grid_cfg_small = (int)std::max<uint64_t>(1, std::min<uint64_t>((s->C + 255) / 256, (uint64_t)s->num_sms * 4));
     int launches = 0;
     if (s->first || s->p == 1) {
@@ -567,19 +837,21 @@ int v2_pass(V2Solver* s, uint64_t* found, cr_solve_stats* stats, std::string* er
     const int grid_pairs = (int)std::max<uint64_t>(1, std::min<uint64_t>((pairs + 7) / 8, (uint64_t)s->num_sms * 8));
     const int grid_cfg = (int)std::max<uint64_t>(1, std::min<uint64_t>((s->C + 7) / 8, (uint64_t)s->num_sms * 8));
     switch (s->k) {
-        case 1: launch_v2_k<1>(d, s->W, grid_pairs, grid_cfg, sm, st); break;
-        case 2: launch_v2_k<2>(d, s->W, grid_pairs, grid_cfg, sm, st); break;
-        case 3: launch_v2_k<3>(d, s->W, grid_pairs, grid_cfg, sm, st); break;
-        default: launch_v2_k<4>(d, s->W, grid_pairs, grid_cfg, sm, st); break;
+        case 1: launches += launch_v2_k<1>(s, d, s->W, grid_pairs, grid_cfg, sm); break;
+        case 2: launches += launch_v2_k<2>(s, d, s->W, grid_pairs, grid_cfg, sm); break;
+        case 3: launches += launch_v2_k<3>(s, d, s->W, grid_pairs, grid_cfg, sm); break;
+        default: launches += launch_v2_k<4>(s, d, s->W, grid_pairs, grid_cfg, sm); break;
     }
     const int grid_apply = (int)std::max<uint64_t>(1, std::min<uint64_t>((pairs + 255) / 256, (uint64_t)s->num_sms * 8));
     k_v2_apply<<<grid_apply, 256, 0, st>>>(s->table, s->marked, s->newval, s->changed, s->C, s->n, s->rwp);
-    launches += 3;
+    launches += 1;
     V2_CUDA(cudaGetLastError());
     V2_CUDA(cudaEventRecord(s->e1, st));
-    V2_CUDA(cudaMemcpyAsync(s->h_pinned, s->counters, 8, cudaMemcpyDeviceToHost, st));
+    V2_CUDA(cudaMemcpyAsync(s->h_pinned, s->counters, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     V2_CUDA(cudaStreamSynchronize(st));
     *found = s->h_pinned[0];
+    s->hstats.child_visits += s->h_pinned[1];
+    s->hstats.entries += s->h_pinned[2];
     float ms = 0;
     cudaEventElapsedTime(&ms, s->e0, s->e1);
     stats->main_ms += ms;
@@ -593,5 +865,7 @@ void v2_verdict(V2Solver* s, unsigned long long* best_key) {
 }
 
 const uint8_t* v2_table(const V2Solver* s) { return s->table; }
+
+cr_v2_hash_stats v2_hash_stats(const V2Solver* s) { return s->hstats; }
 
 }  // namespace crgpu

@@ -21,5 +21,7 @@ int v2_init(V2Solver* s, uint64_t* caps, cr_solve_stats* stats, std::string* err
 int v2_pass(V2Solver* s, uint64_t* found, cr_solve_stats* stats, std::string* err);
 void v2_verdict(V2Solver* s, unsigned long long* best_key);
 const uint8_t* v2_table(const V2Solver* s);
+cr_v2_hash_stats v2_hash_stats(const V2Solver* s);
+int v2_set_hash_capacity(V2Solver* s, uint64_t slots, std::string* err);
 
 }  // namespace crgpu

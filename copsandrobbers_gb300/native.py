@@ -51,6 +51,10 @@ class CrSolveStats(ctypes.Structure):
                 ("slots", ctypes.c_int32), ("resolved", ctypes.c_uint64)]
 
 
+class CrV2HashStats(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_uint64) for f in ("capacity", "child_visits", "entries", "fills")]
+
+
 class CrBatchResult(ctypes.Structure):
     _fields_ = [("solved", ctypes.c_int32), ("status", ctypes.c_int32), ("win", ctypes.c_int32),
                 ("capture_plies", ctypes.c_int32), ("passes", ctypes.c_int32), ("pad", ctypes.c_int32),
@@ -117,6 +121,8 @@ SIGNATURES = {
                                       ctypes.POINTER(CrBatchStats)]),
     "cr_solver_digest": (ctypes.c_int, [ctypes.c_void_p, c_u64p]),
     "cr_solver_load_table_file": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
+    "cr_solver_v2_hash_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(CrV2HashStats)]),
+    "cr_solver_set_v2_hash_capacity": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
     "cr_solver_perfect_game": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64),
                                               ctypes.POINTER(ctypes.c_int32), ctypes.c_int32,
                                               ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),

@@ -127,6 +127,16 @@ class Solver:
         _check(self.ctx.ptr, N.lib().cr_solver_stats(self.ptr, ctypes.byref(s)))
         return s
 
+    def v2_hash_stats(self) -> N.CrV2HashStats:
+        """Cloud-table counts of a v2 solve with p >= 3 (capacity 0 otherwise)."""
+        s = N.CrV2HashStats()
+        _check(self.ctx.ptr, N.lib().cr_solver_v2_hash_stats(self.ptr, ctypes.byref(s)))
+        return s
+
+    def set_v2_hash_capacity(self, slots: int) -> None:
+        """Resize the v2 cloud table (0 = none); results do not depend on its size."""
+        _check(self.ctx.ptr, N.lib().cr_solver_set_v2_hash_capacity(self.ptr, slots))
+
     def states(self, out: np.ndarray | None = None) -> np.ndarray:
         nbytes = int(self.sizes().num_states)
         if out is None:

@@ -157,6 +157,25 @@ int cr_solver_write_table_file(cr_solver* s, const char* path);
  * missing or short, CR_ERR_INVALID when it was written for another solve. */
 int cr_solver_load_table_file(cr_solver* s, const char* path);
 
+/* Deduplication of the robber clouds of a v2 solve with p >= 3.  The reference's
+ * trajectoryDFS (solvers/k_cops_visibility_v2.cpp:243-341) walks every cop trajectory of every
+ * state separately; the device inserts the depth-2 nodes (config, cloud) each pass reaches
+ * into a hash table and evaluates each distinct node once.  Counts accumulate from
+ * cr_solver_init. */
+typedef struct cr_v2_hash_stats {
+    uint64_t capacity;       /* slots of the table; 0 = no table (v1 rules or p < 3) */
+    uint64_t child_visits;   /* non-terminal depth-2 children generated */
+    uint64_t entries;        /* distinct (config, cloud) nodes stored, summed over fills */
+    uint64_t fills;          /* table fills (one per pass, more when depth-1 nodes are chunked) */
+} cr_v2_hash_stats;
+int cr_solver_v2_hash_stats(cr_solver* s, cr_v2_hash_stats* out);
+/* Resize the cloud table of a v2 solve with p >= 3 to `slots` (rounded up to a power of two,
+ * at least 1024; 0 = no table, every depth-2 node is evaluated where it is reached).  A table
+ * smaller than twice the depth-1 nodes fills once per chunk of slots / 2 nodes; nodes a full
+ * table cannot take are evaluated directly, so the results never depend on the size.  The
+ * default is twice the depth-1 nodes, capped at 2^24 slots.  Call between passes only. */
+int cr_solver_set_v2_hash_capacity(cr_solver* s, uint64_t slots);
+
 /* ---- whole solves ---------------------------------------------------------------------- */
 
 /* loadGraphFile..findFinalResult in one call.  states_out (host, may be NULL) receives the

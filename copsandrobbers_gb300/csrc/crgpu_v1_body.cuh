@@ -971,6 +971,51 @@ __device__ CR_BODY_INLINE void cop_seed_body(const V1Dev& d, int col, int nx, un
     t.flush(d, col, L.lane);
 }
 
+// Visits the set flags of f[0 .. C) warp by warp (the sparse producers: push, apply, direct,
+// last column).  Groups of 32 configurations go to the warps round robin (group g to warp
+// g mod W, so that flags clustered in configuration order still spread over all warps); a warp
+// loads the flags of its next kFlagTile groups at once, so they cost one memory round trip
+// instead of one each.  next() hands out, warp-uniformly, each group with a set flag: act has
+// bit l set iff configuration base + l is flagged.
+constexpr int kFlagTile = 16;
+struct FlagScan {
+    const uint8_t* f;
+    size_t C, g0, nwarps;
+    int lane;
+    unsigned mine = 0, groups = 0;
+    bool first = true;
+    __device__ __forceinline__ FlagScan(const uint8_t* f_, size_t C_, unsigned wk, unsigned nwk) : f(f_), C(C_) {
+        lane = threadIdx.x & 31;
+        nwarps = (size_t)nwk * (blockDim.x >> 5);
+        g0 = (size_t)wk * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    }
+    __device__ __forceinline__ bool next(size_t& base, unsigned& act) {
+        while (!groups) {
+            if (!first) g0 += kFlagTile * nwarps;
+            first = false;
+            if (g0 * 32 >= C) return false;
+            uint8_t v[kFlagTile];
+#pragma unroll
+            for (int j = 0; j < kFlagTile; ++j) {
+                const size_t i = (g0 + j * nwarps) * 32 + lane;
+                v[j] = i < C ? f[i] : (uint8_t)0;
+            }
+            mine = 0;   // lane j < kFlagTile holds the ballot of group g0 + j * nwarps
+#pragma unroll
+            for (int j = 0; j < kFlagTile; ++j) {
+                const unsigned b = __ballot_sync(FULL_MASK, v[j] != 0);
+                if (lane == j) mine = b;
+            }
+            groups = __ballot_sync(FULL_MASK, mine != 0u);
+        }
+        const int j = __ffs(groups) - 1;
+        groups &= groups - 1;
+        base = (g0 + j * nwarps) * 32;
+        act = __shfl_sync(FULL_MASK, mine, j);
+        return true;
+    }
+};
+
 // Sparse cop turn, scatter: every non-empty frontier row of column nx is ORed into the
 // candidate rows of its predecessors (the product of the cops' in-neighbour lists).
 template <int K>
@@ -989,10 +1034,10 @@ __device__ CR_BODY_INLINE void cop_push_body(const V1Dev& d, int col, int nx, un
     const uint16_t* CR_RESTRICT radj = d.g.rcol;
     const int np1 = n + 1;
     unsigned err = 0;
-    const size_t stride = (size_t)nwk * blockDim.x;
-    for (size_t base = (size_t)wk * blockDim.x + warp * 32; base < d.C; base += stride) {
-        const size_t mine = base + lane;
-        unsigned act = __ballot_sync(FULL_MASK, mine < d.C && fflag_in[mine]);
+    FlagScan scan(fflag_in, d.C, wk, nwk);
+    size_t base;
+    unsigned act;
+    while (scan.next(base, act)) {
         while (act) {
             const uint32_t cp = (uint32_t)(base + __ffs(act) - 1);
             act &= act - 1;
@@ -1072,10 +1117,10 @@ __device__ CR_BODY_INLINE void cop_apply_body(const V1Dev& d, int col, int nx, u
     uint32_t* wacc = sm + (warp * CPW + L.grp) * (2 * S * rwp);
     uint32_t* wnew = wacc + S * rwp;
     Tally t;
-    const size_t stride = (size_t)nwk * blockDim.x;
-    for (size_t base = (size_t)wk * blockDim.x + warp * 32; base < d.C; base += stride) {
-        const size_t mine = base + L.lane;
-        unsigned act = __ballot_sync(FULL_MASK, mine < d.C && d.cflag[mine]);
+    FlagScan scan(d.cflag, d.C, wk, nwk);
+    size_t base;
+    unsigned act;
+    while (scan.next(base, act)) {
         while (act) {
             bool valid;
             const uint32_t cid = take_flagged<G>(act, base, L, valid);
@@ -1115,10 +1160,10 @@ __device__ CR_BODY_INLINE void direct_body(const V1Dev& d, int col, int nx, unsi
     uint32_t* wnew = wacc + S * rwp;
     const uint8_t* CR_RESTRICT fflag_in = d.fflag + (size_t)nx * d.C;
     Tally t;
-    const size_t stride = (size_t)nwk * blockDim.x;
-    for (size_t base = (size_t)wk * blockDim.x + warp * 32; base < d.C; base += stride) {
-        const size_t mine = base + L.lane;
-        unsigned act = __ballot_sync(FULL_MASK, mine < d.C && fflag_in[mine]);
+    FlagScan scan(fflag_in, d.C, wk, nwk);
+    size_t base;
+    unsigned act;
+    while (scan.next(base, act)) {
         while (act) {
             bool valid;
             const uint32_t cid = take_flagged<G>(act, base, L, valid);
@@ -1185,10 +1230,10 @@ __device__ CR_BODY_INLINE void and_body(const V1Dev& d, int col, unsigned wk, un
     }
     const int avg_deg = max(1, (nnz + n - 1) / n);
     Tally t;
-    const size_t stride = (size_t)nwk * blockDim.x;
-    for (size_t base = (size_t)wk * blockDim.x + warp * 32; base < d.C; base += stride) {
-        const size_t mine = base + L.lane;
-        unsigned act = __ballot_sync(FULL_MASK, mine < d.C && fflag0[mine]);
+    FlagScan scan(fflag0, d.C, wk, nwk);
+    size_t base;
+    unsigned act;
+    while (scan.next(base, act)) {
         while (act) {
             bool valid;
             const uint32_t cid = take_flagged<G>(act, base, L, valid);

@@ -35,6 +35,7 @@ void launch_popcount(const uint32_t* plane, size_t words, unsigned long long* ou
 int max_cop_blocks_per_sm(int k, int rwp, int S);
 bool pull_supported(int S, int rwp);
 int cop_launches(int direct);
+int cop_launches_k(int direct, int k, bool sep);
 size_t cop_smem_bytes(int S, int rwp);
 size_t and_smem_bytes(int S, int rwp, int n);
 void launch_unrank(const uint32_t* B, int n, int k, uint32_t C, uint16_t* out, int grid, cudaStream_t st);
@@ -76,6 +77,7 @@ struct cr_solver {
     uint32_t* d_front = nullptr;
     uint8_t* d_fflag = nullptr;
     uint32_t* d_cand = nullptr;
+    uint32_t* d_h1 = nullptr;   // k = 3: H1 rows of the separable dense cop turn
     uint8_t* d_cflag = nullptr;
     uint32_t* d_rrp = nullptr;
     uint16_t* d_rcol = nullptr;
@@ -226,6 +228,14 @@ int cr_graph_parse(const char* text, size_t len, int32_t* n_out, uint32_t* row_p
 
 static int slots_for(int n) { (void)n; return 2; }
 
+// H1 rows of the separable dense cop turn (k = 3): every pair {x <= y} times every vertex,
+// one frontier row each; about 3/8 of the table's bytes.  0 when the turn keeps the
+// tuple-gathering form.
+static uint64_t h1_bytes(int n, int k, int S, int rwp) {
+    if (k != 3 || !pull_supported(S, rwp)) return 0;
+    return (uint64_t)n * (n + 1) / 2 * n * S * rwp * 4;
+}
+
 static void layout(int n, int k, int p, int rules, int S, uint64_t* C, int* cols, int* rw, int* rwp) {
     *C = binom_u64((int64_t)n + k - 1, k);
     *cols = rules == CR_RULES_V2 ? 1 : 2 * p;
@@ -245,6 +255,7 @@ uint64_t cr_solver_footprint(int32_t n, int32_t k, int32_t p, int32_t rules) {
     b += (uint64_t)cols * C * rwp * 4;                   // marked
     b += (uint64_t)cols * C * S * rwp * 4;               // frontiers
     b += C * S * rwp * 4 + C;                            // push-mode candidate rows and flags
+    b += h1_bytes(n, k, S, rwp);                         // separable dense cop turn (k = 3)
     b += (uint64_t)cols * C;                             // flags
     b += C * (uint64_t)k * 2;                            // configs
     b += (uint64_t)n * rwp * 4 * 3 + (uint64_t)k * (n + 1) * 4 + (1u << 16);
@@ -265,7 +276,7 @@ static void free_v1(cr_solver* s) {
     void* ptrs[] = {s->d_rp, s->d_col, s->d_binom, s->d_configs, s->d_hop, s->d_table,
                     s->d_marked, s->d_front, s->d_fflag, s->d_meta, s->d_counters, s->d_err,
                     s->d_heads, s->d_trans, s->d_cand, s->d_cflag, s->d_rrp, s->d_rcol, s->d_nbr, s->d_iso, s->d_rhop, s->d_cover,
-                    s->d_crp, s->d_ccol, s->d_ciso};
+                    s->d_crp, s->d_ccol, s->d_ciso, s->d_h1};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     s->d_rp = nullptr; s->d_col = nullptr; s->d_binom = nullptr; s->d_configs = nullptr;
@@ -274,7 +285,7 @@ static void free_v1(cr_solver* s) {
     s->d_heads = nullptr; s->d_trans = nullptr; s->d_cand = nullptr; s->d_cflag = nullptr;
     s->d_rrp = nullptr; s->d_rcol = nullptr; s->d_nbr = nullptr; s->d_iso = nullptr; s->d_rhop = nullptr;
     s->d_cover = nullptr;
-    s->d_crp = nullptr; s->d_ccol = nullptr; s->d_ciso = nullptr;
+    s->d_crp = nullptr; s->d_ccol = nullptr; s->d_ciso = nullptr; s->d_h1 = nullptr;
     if (s->h_pinned) cudaFreeHost(s->h_pinned);
     s->h_pinned = nullptr;
     cudaEvent_t evs[] = {s->ev0, s->ev1, s->evc0, s->evc1};
@@ -315,6 +326,7 @@ static V1Dev dev_view(const cr_solver* s) {
     d.front = s->d_front;
     d.fflag = s->d_fflag;
     d.cand = s->d_cand;
+    d.h1 = s->d_h1;
     d.cflag = s->d_cflag;
     d.meta = s->d_meta;
     d.pass_new = s->d_counters;
@@ -354,6 +366,7 @@ static int alloc_v1(cr_solver* s) {
     CR_CUDA(ctx, cudaMalloc(&s->d_cflag, C));
     CR_CUDA(ctx, cudaMemsetAsync(s->d_cand, 0, C * s->S * s->rwp * 4, ctx->stream));
     CR_CUDA(ctx, cudaMemsetAsync(s->d_cflag, 0, C, ctx->stream));
+    if (const uint64_t hb = h1_bytes(s->n, s->k, s->S, s->rwp)) CR_CUDA(ctx, cudaMalloc(&s->d_h1, hb));
     CR_CUDA(ctx, cudaMalloc(&s->d_hop, (size_t)s->n * s->rwp * 4));
     std::vector<uint32_t> hop = hop_masks(s);
     CR_CUDA(ctx, cudaMemcpyAsync(s->d_hop, hop.data(), hop.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
@@ -702,7 +715,7 @@ static int v1_pass(cr_solver* s, uint64_t* found) {
     CR_CUDA(ctx, cudaStreamSynchronize(st));
     int per_pass = s->cols;  // prep kernels
     for (int col = 0; col < s->cols; ++col)
-        per_pass += col % 2 == 0 ? cop_launches(0) : (col < s->cols - 1 ? cop_launches(1) : 1);
+        per_pass += col % 2 == 0 ? cop_launches_k(0, s->k, s->d_h1 != nullptr) : (col < s->cols - 1 ? cop_launches(1) : 1);
     s->stats.kernel_launches += per_pass;
     *found = s->h_pinned[0];
     return CR_OK;
@@ -748,6 +761,8 @@ static int grow_slots_and_replay(cr_solver* s) {
     s->d_front = nullptr;
     cudaFree(s->d_cand);
     s->d_cand = nullptr;
+    if (s->d_h1) cudaFree(s->d_h1);
+    s->d_h1 = nullptr;
     if (s->pass_graph) cudaGraphExecDestroy(s->pass_graph);
     s->pass_graph = nullptr;
     if (s->run_graph) cudaGraphExecDestroy(s->run_graph);
@@ -759,6 +774,7 @@ static int grow_slots_and_replay(cr_solver* s) {
     CR_CUDA(ctx, cudaMalloc(&s->d_cand, (size_t)s->C * s->S * s->rwp * 4));
     CR_CUDA(ctx, cudaMemsetAsync(s->d_cand, 0, (size_t)s->C * s->S * s->rwp * 4, ctx->stream));
     CR_CUDA(ctx, cudaMemsetAsync(s->d_cflag, 0, s->C, ctx->stream));
+    if (const uint64_t hb = h1_bytes(s->n, s->k, s->S, s->rwp)) CR_CUDA(ctx, cudaMalloc(&s->d_h1, hb));
     const int per_sm = max_cop_blocks_per_sm(s->k, s->rwp, s->S);
     s->grid_cop = (int)std::max<uint64_t>(1, std::min<uint64_t>((s->C + 7) / 8, (uint64_t)ctx->num_sms * per_sm));
     uint64_t caps;
@@ -880,7 +896,7 @@ static int v1_run_on_device(cr_solver* s) {
     CR_CUDA(ctx, cudaMemcpy(h.data(), s->d_hist, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost));
     int per_pass = s->cols + 1;  // prep kernels and the loop's pass end
     for (int col = 0; col < s->cols; ++col)
-        per_pass += col % 2 == 0 ? cop_launches(0) : (col < s->cols - 1 ? cop_launches(1) : 1);
+        per_pass += col % 2 == 0 ? cop_launches_k(0, s->k, s->d_h1 != nullptr) : (col < s->cols - 1 ? cop_launches(1) : 1);
     s->stats.kernel_launches += (int64_t)per_pass * n;
     if (bits & kErrRank) return fail(ctx, CR_ERR_INTERNAL, "successor rank out of range");
     if (bits & kErrSlot) {

@@ -89,6 +89,9 @@ struct V1Dev {
     uint32_t* front;
     uint8_t* fflag;
     uint32_t* cand;           // [C][S][rwp]: push-mode OR of successor frontier rows
+    // k = 3 dense cop turns: H1 rows [P][n][S][rwp], P = n(n+1)/2 pairs {x <= y}; H1[{x,y}][c]
+    // = OR over z in N(c) of the frontier row of sort(x, y, z).  Null = the tuple-gathering pull.
+    uint32_t* h1 = nullptr;
     uint8_t* cflag;           // [C]: 1 = cand row non-empty
     ColMeta* meta;            // [cols]
     unsigned long long* pass_new;

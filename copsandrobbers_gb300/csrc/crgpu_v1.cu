@@ -52,6 +52,14 @@ template <int K, int NWP, int G>
 __global__ void __launch_bounds__(256) k_cop_pull(V1Dev d, int col, int nx) {
     cop_pull_body<K, NWP, G>(d, col, nx, blockIdx.x, gridDim.x);
 }
+template <int NWP, int G>
+__global__ void __launch_bounds__(256) k_pair_h1(V1Dev d, int nx) {
+    pair_h1_body<NWP, G>(d, nx, blockIdx.x, gridDim.x);
+}
+template <int NWP, int G>
+__global__ void __launch_bounds__(256) k_sep_pull(V1Dev d, int col, int nx) {
+    sep_pull_body<NWP, G>(d, col, nx, blockIdx.x, gridDim.x);
+}
 template <int K, int G>
 __global__ void __launch_bounds__(256) k_cop_seed(V1Dev d, int col, int nx) {
     cop_seed_body<K, G>(d, col, nx, blockIdx.x, gridDim.x);
@@ -138,6 +146,32 @@ static void launch_pull_g(const V1Dev& d, int col, int nx, int grid, cudaStream_
     }
 }
 
+template <int NWP, int G>
+static void launch_sep_ng(const V1Dev& d, int col, int nx, int grid, cudaStream_t st) {
+    const size_t sm = cop_smem_bytes(d.S, d.g.rwp);
+    k_pair_h1<NWP, G><<<grid, 256, sm + (size_t)rank_table_words(3, d.g.n) * 4, st>>>(d, nx);
+    k_sep_pull<NWP, G><<<grid, 256, sm, st>>>(d, col, nx);
+}
+
+// The separable k = 3 dense cop turn (same word and lane shapes as the pull).
+template <int G>
+static void launch_sep_g(const V1Dev& d, int col, int nx, int grid, cudaStream_t st) {
+    switch (pull_words(d.S, d.g.rwp)) {
+        case 2: if (G == 4) launch_sep_ng<2, 4>(d, col, nx, grid, st); break;
+        case 4: if (G == 4) launch_sep_ng<4, 4>(d, col, nx, grid, st); break;
+        case 8: if (G == 4) launch_sep_ng<8, 4>(d, col, nx, grid, st); break;
+        case 16:
+            if (G == 4) launch_sep_ng<16, 4>(d, col, nx, grid, st);
+            else launch_sep_ng<16, 8>(d, col, nx, grid, st);
+            break;
+        default:
+            if (G == 4) launch_sep_ng<32, 4>(d, col, nx, grid, st);
+            else if (G == 8) launch_sep_ng<32, 8>(d, col, nx, grid, st);
+            else launch_sep_ng<32, 16>(d, col, nx, grid, st);
+            break;
+    }
+}
+
 template <int G>
 static void launch_rows_g(const V1Dev& d, int col, int nx, int direct, int grid, cudaStream_t st) {
     const size_t sm = cop_smem_bytes(d.S, d.g.rwp);
@@ -168,6 +202,13 @@ static void launch_cop_k(const V1Dev& d, int col, int nx, int grid, cudaStream_t
         case 8: launch_pull_g<K, 8>(d, col, nx, grid, st); break;
         default: launch_pull_g<K, 16>(d, col, nx, grid, st); break;
     }
+    if (K == 3 && d.h1) {
+        switch (group_lanes(d.g.rwp)) {
+            case 4: launch_sep_g<4>(d, col, nx, grid, st); break;
+            case 8: launch_sep_g<8>(d, col, nx, grid, st); break;
+            default: launch_sep_g<16>(d, col, nx, grid, st); break;
+        }
+    }
     k_cop_push<K><<<grid, 256, (size_t)8 * d.S * d.g.rwp * 4, st>>>(d, col, nx);
     launch_rows(d, col, nx, 0, grid, st);
 }
@@ -188,6 +229,7 @@ void launch_cop(const V1Dev& d, int col, int nx, int direct, int grid, cudaStrea
 }
 
 int cop_launches(int direct) { return direct ? 1 : 4; }
+int cop_launches_k(int direct, int k, bool sep) { return direct ? 1 : (k == 3 && sep ? 6 : 4); }
 
 // Shared-memory words the last-column body stages the graph in: transposed hop rows, row
 // pointers and neighbour lists.

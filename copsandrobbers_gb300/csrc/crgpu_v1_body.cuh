@@ -782,6 +782,7 @@ __device__ CR_BODY_INLINE void cop_pull_body(const V1Dev& d, int col, int nx, un
     const ColMeta mi = d.meta[nx];
     if (mi.hi < mi.lo) return;                              // empty frontier: nothing changes
     if (mi.seed || frontier_sparse(mi, d.C)) return;       // the seed or push form handles it
+    if (K == 3 && d.h1) return;                             // the separable form handles it
     const int base_in = mi.base;
     const int s_used = min(mi.hi - base_in + 1, S);
     const int nwords = s_used * rwp;
@@ -919,6 +920,190 @@ __device__ CR_BODY_INLINE void cop_pull_body(const V1Dev& d, int col, int nx, un
             }
             group_or<NWP, G>(acc, gl, wacc, need ? nwords : 0);
         }
+        __syncwarp();
+        emit_row<G>(d, cid, need, col, m, wacc, wnew, base_in, s_used, out_base, append, L, t);
+    }
+    t.flush(d, col, L.lane);
+}
+
+// Pair index of the multiset {x <= y} among all pairs in lexicographic order, and its inverse.
+__device__ __forceinline__ uint32_t pair_index(int x, int y, int n) {
+    return (uint32_t)(x * (2 * n - x + 1) / 2 + (y - x));
+}
+__device__ __forceinline__ void pair_of(uint32_t q, int n, int& x, int& y) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if ((uint32_t)(mid * (2 * n - mid + 1) / 2) <= q) lo = mid;
+        else hi = mid - 1;
+    }
+    x = lo;
+    y = lo + (int)(q - (uint32_t)(lo * (2 * n - lo + 1) / 2));
+}
+
+// Dense cop turn for k = 3 in separable form.  The OR over T(C) of the frontier rows F[C'],
+// C' = sort(x, y, z) with x in N(c1), y in N(c2), z in N(c3), splits into two stages:
+//   H1[{x, y}][c] = OR over z in N(c) of F[sort(x, y, z)]             (pair_h1_body)
+//   acc(C)        = OR over x in N(c1), y in N(c2) of H1[{x, y}][c3]  (sep_pull_body)
+// so a configuration reads deg^2 rows of H1 (consecutive configurations read consecutive
+// rows) instead of ranking and gathering deg^3 successor tuples, and the ranks are taken
+// once per (pair, z) instead of once per tuple.  OR is exact, so the marks are the pull's.
+// Stage 1: a lane group per H1 row, its lanes over z in N(c), reduced by halving.
+template <int NWP, int G>
+__device__ CR_BODY_INLINE void pair_h1_body(const V1Dev& d, int nx, unsigned wk, unsigned nwk) {
+    extern __shared__ uint32_t sm[];
+    constexpr int K = 3;
+    constexpr int CPW = 32 / G;
+    const int warp = threadIdx.x >> 5;
+    const Lanes<G> L(threadIdx.x & 31);
+    const int gl = L.glane;
+    const int n = d.g.n, rwp = d.g.rwp, S = d.S;
+    const ColMeta mi = d.meta[nx];
+    if (!d.h1 || mi.hi < mi.lo || mi.seed || frontier_sparse(mi, d.C)) return;
+    const int s_used = min(mi.hi - mi.base + 1, S);
+    const int nwords = s_used * rwp;
+    const int np1 = n + 1;
+    uint32_t* sB = sm;
+    for (int i = threadIdx.x; i < K * np1; i += blockDim.x) sB[i] = CR_LDG(&d.binom[i]);
+    __syncthreads();
+    uint32_t* wacc = sm + rank_table_words(K, n) + (warp * CPW + L.grp) * (2 * S * rwp);
+    const uint32_t* CR_RESTRICT fin = d.front + (size_t)nx * d.C * S * rwp;
+    const uint8_t* CR_RESTRICT fflag_in = d.fflag + (size_t)nx * d.C;
+    const uint32_t* CR_RESTRICT rp = cop_rows(d.g);
+    const uint16_t* CR_RESTRICT adj = cop_cols(d.g);
+    const bool vec4 = (rwp & 3) == 0;
+    unsigned err = 0;
+    const size_t rows = (size_t)n * (n + 1) / 2 * n;
+    const size_t step = (size_t)nwk * (blockDim.x >> 5) * CPW;
+    for (size_t rb = ((size_t)wk * (blockDim.x >> 5) + warp) * CPW; rb < rows; rb += step) {
+        const size_t row = rb + L.grp;
+        const bool ok = row < rows;
+        uint32_t acc[NWP];
+#pragma unroll
+        for (int i = 0; i < NWP; ++i) acc[i] = 0u;
+        int x = 0, y = 0, lo = 0, dg = 0;
+        if (ok) {
+            const uint32_t q = (uint32_t)(row / n);
+            const int c = (int)(row - (size_t)q * n);
+            pair_of(q, n, x, y);
+            lo = CR_LDG(&rp[c]);
+            dg = CR_LDG(&rp[c + 1]) - lo;
+        }
+        for (int t = gl; t < dg; t += G) {
+            const int z = CR_LDG(&adj[lo + t]);
+            int cc[K];
+            cc[0] = z < x ? z : x;
+            cc[1] = z < x ? x : (z < y ? z : y);
+            cc[2] = z < y ? y : z;
+            const uint32_t s = rank_s<K>(cc, sB, np1);
+            if (s >= d.C) { err |= kErrRank; continue; }
+            if (!CR_LDG(&fflag_in[s])) continue;
+            const uint32_t* fr = fin + (size_t)s * S * rwp;
+            if (vec4) {
+#pragma unroll
+                for (int w = 0; w < NWP; w += 4) {
+                    if (w < nwords) {
+                        const uint4 v = CR_LDG(reinterpret_cast<const uint4*>(fr + w));
+                        acc[w] |= v.x; acc[w + 1] |= v.y; acc[w + 2] |= v.z; acc[w + 3] |= v.w;
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int w = 0; w < NWP; ++w)
+                    if (w < nwords) acc[w] |= CR_LDG(fr + w);
+            }
+        }
+        group_or<NWP, G>(acc, gl, wacc, ok ? nwords : 0);
+        __syncwarp();
+        if (ok) {
+            uint32_t* out = d.h1 + row * S * rwp;
+            for (int e = gl; e < nwords; e += G) out[e] = wacc[e];
+        }
+        __syncwarp();
+    }
+    err = __reduce_or_sync(FULL_MASK, err);
+    if ((threadIdx.x & 31) == 0 && err) atomicOr(d.err, err);
+}
+
+// Stage 2: a lane group per configuration, its lanes over the deg^2 pairs (x, y).
+template <int NWP, int G>
+__device__ CR_BODY_INLINE void sep_pull_body(const V1Dev& d, int col, int nx, unsigned wk, unsigned nwk) {
+    extern __shared__ uint32_t sm[];
+    constexpr int K = 3;
+    constexpr int CPW = 32 / G;
+    const int warp = threadIdx.x >> 5;
+    const Lanes<G> L(threadIdx.x & 31);
+    const int gl = L.glane;
+    const int n = d.g.n, rw = d.g.rw, rwp = d.g.rwp, S = d.S;
+    const ColMeta mi = d.meta[nx];
+    if (!d.h1 || mi.hi < mi.lo || mi.seed || frontier_sparse(mi, d.C)) return;
+    const int base_in = mi.base;
+    const int s_used = min(mi.hi - base_in + 1, S);
+    const int nwords = s_used * rwp;
+    const int out_base = d.meta[col].base;
+    const int append = d.meta[col].append;
+    uint32_t* wacc = sm + (warp * CPW + L.grp) * (2 * S * rwp);
+    uint32_t* wnew = wacc + S * rwp;
+    const uint32_t* CR_RESTRICT rp = cop_rows(d.g);
+    const uint16_t* CR_RESTRICT adj = cop_cols(d.g);
+    const uint32_t* CR_RESTRICT h1 = d.h1;
+    const bool vec4 = (rwp & 3) == 0;
+    const size_t rstride = (size_t)S * rwp;
+    Tally t;
+    const size_t step = (size_t)nwk * (blockDim.x >> 5) * CPW;
+    for (size_t cb = ((size_t)wk * (blockDim.x >> 5) + warp) * CPW; cb < d.C; cb += step) {
+        const uint32_t cid = (uint32_t)(cb + L.grp);
+        const bool ok = cid < d.C;
+        const uint32_t vm = (ok && gl < rw) ? valid_mask(n, gl) : 0u;
+        const uint32_t m = (ok && gl < rw) ? d.marked[((size_t)col * d.C + cid) * rwp + gl] : 0u;
+        const bool full = L.all(m == vm);
+        const bool need = ok && !full;
+        if (!__any_sync(FULL_MASK, need)) continue;
+        int lo0 = 0, dg0 = 0, lo1 = 0, dg1 = 0, c3 = 0;
+        if (need) {
+            const uint16_t* cc = d.configs + (size_t)cid * K;
+            const int v0 = cc[0], v1 = cc[1];
+            c3 = cc[2];
+            lo0 = CR_LDG(&rp[v0]);
+            dg0 = CR_LDG(&rp[v0 + 1]) - lo0;
+            lo1 = CR_LDG(&rp[v1]);
+            dg1 = CR_LDG(&rp[v1 + 1]) - lo1;
+        }
+        const int T = dg0 * dg1;
+        uint32_t acc[NWP];
+#pragma unroll
+        for (int i = 0; i < NWP; ++i) acc[i] = 0u;
+        // odometer over N(c1) x N(c2): this lane starts at pair gl and steps by G
+        int i0 = 0, i1 = 0;
+        if (T > 0) {
+            i0 = gl / dg1;
+            i1 = gl - i0 * dg1;
+        }
+#pragma unroll 2
+        for (int tt = gl; tt < T; tt += G) {
+            const int xa = CR_LDG(&adj[lo0 + i0]), yb = CR_LDG(&adj[lo1 + i1]);
+            const uint32_t q = xa <= yb ? pair_index(xa, yb, n) : pair_index(yb, xa, n);
+            const uint32_t* hr = h1 + ((size_t)q * n + c3) * rstride;
+            if (vec4) {
+#pragma unroll
+                for (int w = 0; w < NWP; w += 4) {
+                    if (w < nwords) {
+                        const uint4 v = CR_LDG(reinterpret_cast<const uint4*>(hr + w));
+                        acc[w] |= v.x; acc[w + 1] |= v.y; acc[w + 2] |= v.z; acc[w + 3] |= v.w;
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int w = 0; w < NWP; ++w)
+                    if (w < nwords) acc[w] |= CR_LDG(hr + w);
+            }
+            i1 += G;
+            while (i1 >= dg1 && i0 < dg0) {
+                i1 -= dg1;
+                ++i0;
+            }
+        }
+        group_or<NWP, G>(acc, gl, wacc, need ? nwords : 0);
         __syncwarp();
         emit_row<G>(d, cid, need, col, m, wacc, wnew, base_in, s_used, out_base, append, L, t);
     }

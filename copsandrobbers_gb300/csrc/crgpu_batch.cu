@@ -83,7 +83,7 @@ __host__ __device__ inline uint64_t binom_dev(int64_t n, int64_t k) {
 
 // Byte offsets of one (n, k, p) solve inside a slot.
 struct JobLayout {
-    size_t binom, configs, nbr, iso, hop, rhop, table, marked, front, fflag, cand, cflag, meta,
+    size_t binom, configs, nbr, iso, hop, rhop, table, marked, front, h1, fflag, cand, cflag, meta,
         counters, err, total;
 };
 
@@ -106,6 +106,9 @@ __host__ __device__ inline JobLayout job_layout(int n, int k, int p, int S) {
     L.table = take(C * (size_t)n * cols);
     L.marked = take((size_t)cols * C * rwp * 4);
     L.front = take((size_t)cols * C * S * rwp * 4);
+    // k = 3: rows of the separable dense cop turn (written before they are read each pass,
+    // so they sit outside the regions the block zeroes)
+    L.h1 = take(k == 3 ? (size_t)n * (n + 1) / 2 * n * S * rwp * 4 : 0);
     L.fflag = take((size_t)cols * C);
     L.cand = take(C * S * rwp * 4);
     L.cflag = take(C);
@@ -172,6 +175,7 @@ __device__ int solve_job(const BatchDev& b, unsigned char* slot, int gi, int jr,
     d.front = reinterpret_cast<uint32_t*>(slot + L.front);
     d.fflag = slot + L.fflag;
     d.cand = reinterpret_cast<uint32_t*>(slot + L.cand);
+    d.h1 = K == 3 ? reinterpret_cast<uint32_t*>(slot + L.h1) : nullptr;
     d.cflag = slot + L.cflag;
     d.meta = reinterpret_cast<ColMeta*>(slot + L.meta);
     d.pass_new = reinterpret_cast<unsigned long long*>(slot + L.counters);
@@ -273,6 +277,12 @@ __device__ int solve_job(const BatchDev& b, unsigned char* slot, int gi, int jr,
                 __syncthreads();
                 cop_pull_body<K, NWP, G>(d, col, nx, 0, 1);
                 __syncthreads();
+                if (K == 3) {
+                    pair_h1_body<NWP, G>(d, nx, 0, 1);
+                    __syncthreads();
+                    sep_pull_body<NWP, G>(d, col, nx, 0, 1);
+                    __syncthreads();
+                }
                 cop_push_body<K>(d, col, nx, 0, 1);
                 __syncthreads();
                 cop_apply_body<G>(d, col, nx, 0, 1);

@@ -75,3 +75,27 @@ def test_v1_has_no_cloud_table(gpu_ctx):
     with Solver(gpu_ctx, g, 2, 3, N.CR_RULES_V1) as s:
         s.set_v2_hash_capacity(4096)            # ignored: v1 rules keep no clouds
         assert s.v2_hash_stats().capacity == 0
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("slots", [None, 0])
+def test_limited_visibility_workload_full_size(gpu_ctx, slots):
+    """The limited-visibility workload itself (Delaunay-thinned n=199, k=2, p=3, 3.96 M states)
+    against the oracle's table (tests/golden/v2_large.json, made by make_v2_large.py; the
+    reference's own v2 solver does not finish this graph), with and without the cloud table."""
+    import hashlib
+    import json
+    import os
+    here = os.path.join(os.path.dirname(__file__), "golden")
+    case = json.load(open(os.path.join(here, "v2_large.json")))["delaunay_n199_k2_p3"]
+    g = G.load_matrix(os.path.join(here, case["matrix"]))
+    with Solver(gpu_ctx, g, case["k"], case["p"], N.CR_RULES_V2) as s:
+        if slots is not None:
+            s.set_v2_hash_capacity(slots)
+        assert s.init() == case["base_captures"]
+        assert s.run() == case["pass_counts"]
+        v = s.verdict()
+        st = s.states()
+    assert hashlib.sha256(st.tobytes()).hexdigest() == case["sha_states"]
+    assert ("WIN" if v.win else "LOSS") == case["result"]
+    assert v.best_config == case["best_config"]

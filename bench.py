@@ -210,7 +210,7 @@ def limited_visibility_workload(ctx) -> dict:
             "reference": "the reference v2 solver did not finish this graph at p=2 within 600 s"}
 
 
-def serving_workload(count: int, rate: float, workers: int = 8) -> dict:
+def serving_workload(count: int, rate: float, workers: int = 16) -> dict:
     """A seeded Poisson stream of solve requests through the solve server (cr_server_*):
     4-regular / G(n, 4/(n-1)) / Delaunay-thinned graphs, n log-uniform in [20, 400], k in
     {1, 2, 3}, 10% with visibility period p in [2, 4]; admission by device footprint, tables
@@ -441,7 +441,7 @@ def main() -> None:
     ap.add_argument("--headline-only", action="store_true",
                     help="skip the batched, limited-visibility and serving workloads")
     ap.add_argument("--serving-requests", type=int, default=2000)
-    ap.add_argument("--serving-rate", type=float, default=60.0, help="requests per second")
+    ap.add_argument("--serving-rate", type=float, default=45.0, help="requests per second")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -1442,14 +1442,21 @@ __device__ CR_BODY_INLINE void and_body(const V1Dev& d, int col, unsigned wk, un
             const int c_touch = marked0 * rwp + (P1 ? marked0 * avg_deg : open);
             const bool touch_form = c_touch < c_test && c_touch <= c_block;
             const bool block_form = !touch_form && c_block < c_test;
-            if (__any_sync(FULL_MASK, touch_form && need)) {
-                // each lane ORs the transposed hop rows of the marked vertices in its own word;
-                // the group reduces the rows by halving into wtouch
+            // block form with groups of up to 4 lanes (n <= 128): each lane walks the unmarked
+            // vertices of its own word and ORs whole rows, like the touch form; wider groups
+            // keep one pass per lane over the whole list (clustered unmarked vertices would
+            // leave a few lanes with all the rows)
+            constexpr bool kBlockRows = G <= 4;
+            const bool rows_form = touch_form || (kBlockRows && block_form);
+            if (__any_sync(FULL_MASK, rows_form && need)) {
+                // each lane ORs the transposed hop rows of the marked (touch form) or unmarked
+                // (block form) vertices of its own word; the group reduces the rows by halving
+                // into wtouch: the touched, or the blocked, robbers
                 uint32_t acc[G];
 #pragma unroll
                 for (int i = 0; i < G; ++i) acc[i] = 0u;
-                if (touch_form && need && gl < rw) {
-                    uint32_t mb = m0;
+                if (rows_form && need && gl < rw) {
+                    uint32_t mb = touch_form ? m0 : (~m0 & vm);
                     while (mb) {
                         const int v = gl * 32 + __ffs(mb) - 1;
                         mb &= mb - 1;
@@ -1459,7 +1466,7 @@ __device__ CR_BODY_INLINE void and_body(const V1Dev& d, int col, unsigned wk, un
                             if (w < rwp) acc[w] |= row[w];
                     }
                 }
-                group_or<G, G>(acc, gl, wtouch, (touch_form && need) ? rwp : 0);
+                group_or<G, G>(acc, gl, wtouch, (rows_form && need) ? rwp : 0);
             }
             __syncwarp();
             if (need && gl < rw) {
@@ -1469,16 +1476,20 @@ __device__ CR_BODY_INLINE void and_body(const V1Dev& d, int col, unsigned wk, un
                 uint32_t cand = ~mc & vm;
                 if (touch_form) cand &= wtouch[gl] | CR_LDG(&d.g.isolated[gl]);
                 if (block_form) {
-                    uint32_t blocked = 0;
-                    for (int w2 = 0; w2 < rw; ++w2) {
-                        uint32_t ub = ~wm0[w2] & valid_mask(n, w2);
-                        while (ub) {
-                            const int u = w2 * 32 + __ffs(ub) - 1;
-                            ub &= ub - 1;
-                            blocked |= rhop[(size_t)u * rwp + gl];
+                    if (kBlockRows) {
+                        cand &= ~wtouch[gl];
+                    } else {
+                        uint32_t blocked = 0;
+                        for (int w2 = 0; w2 < rw; ++w2) {
+                            uint32_t ub = ~wm0[w2] & valid_mask(n, w2);
+                            while (ub) {
+                                const int u = w2 * 32 + __ffs(ub) - 1;
+                                ub &= ub - 1;
+                                blocked |= rhop[(size_t)u * rwp + gl];
+                            }
                         }
+                        cand &= ~blocked;
                     }
-                    cand &= ~blocked;
                 }
                 while (cand) {
                     const int r = gl * 32 + __ffs(cand) - 1;

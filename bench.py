@@ -42,6 +42,23 @@ LARGE = {"workload": "large single solve: seeded connected 4-regular graph, n=25
 METRIC = "resolved states/s"
 
 
+def max_over_ranks(ms: float, world: int, device: str = "cuda") -> float:
+    """The slowest rank's time (every rank gets it): the job's time for N replicas."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([ms], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replicas_value(states_per_step: int, steps: int, world: int, max_ms: float) -> float:
+    """Whole-job throughput of N replicas: the states all ranks solved over the slowest rank's time."""
+    return states_per_step * steps * world / (max_ms / 1e3)
+
+
 def dist_info():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -322,12 +339,8 @@ def run_gpu(args) -> None:
         ev1.record(stream)
         torch.cuda.synchronize()
     barrier()
-    ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = S * args.steps * world / (ms / 1e3)
+    ms = max_over_ranks(ev0.elapsed_time(ev1), world)
+    value = replicas_value(S, args.steps, world, ms)
     verdict = solver.verdict()
 
     # roofline of the dominant kernel, k_init_pass1 (initializeCaptures and pass 1 in one
@@ -388,12 +401,8 @@ def run_gpu(args) -> None:
     e1.record(stream)
     torch.cuda.synchronize()
     barrier()
-    e2e_ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([e2e_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e_value = S * args.steps * world / (e2e_ms / 1e3)
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1), world)
+    e2e_value = replicas_value(S, args.steps, world, e2e_ms)
 
     line = None
     extra = {}

@@ -179,6 +179,7 @@ __device__ __forceinline__ Mask<W> expand(const Mask<W>& m, const uint32_t* snbr
 template <int K>
 struct Moves {
     int lo[K], dg[K], T;
+    int idx[K];   // odometer of the next successor tuple (last cop fastest)
 };
 
 template <int K>
@@ -189,7 +190,28 @@ __device__ __forceinline__ void moves_of(Moves<K>& mv, const int (&c)[K], const 
         mv.lo[i] = __ldg(&rp[c[i]]);
         mv.dg[i] = __ldg(&rp[c[i] + 1]) - mv.lo[i];
         mv.T *= mv.dg[i];
+        mv.idx[i] = 0;
     }
+}
+
+// The successor tuple at the odometer (the same tuple move_target gives for the running
+// index), then the odometer steps on: the sequential walks need no division per tuple.
+template <int K>
+__device__ __forceinline__ uint32_t next_target(Moves<K>& mv, const uint16_t* __restrict__ adj,
+                                                const uint32_t* __restrict__ B, int np1, int (&c)[K]) {
+#pragma unroll
+    for (int i = 0; i < K; ++i) c[i] = __ldg(&adj[mv.lo[i] + mv.idx[i]]);
+    bool carry = true;
+#pragma unroll
+    for (int i = K - 1; i >= 0; --i) {
+        if (carry) {
+            ++mv.idx[i];
+            carry = mv.idx[i] >= mv.dg[i];
+            if (carry) mv.idx[i] = 0;
+        }
+    }
+    sort_small<K>(c);
+    return config_rank<K>(c, B, np1);
 }
 
 template <int K>
@@ -250,9 +272,9 @@ __device__ int subtree_min(const V2Dev& d, const int (&c2)[K], const Mask<W>& V2
         Frame<W, K>& f = st[top];
         const int dc = top + 3;  // depth of the child about to be tried
         if (f.t >= f.mv.T || 2 * dc - 1 >= best) { --top; continue; }
-        const int t = f.t++;
+        ++f.t;
         int c[K];
-        const uint32_t cid = move_target<K>(f.mv, t, d.col, d.binom, np1, c);
+        const uint32_t cid = next_target<K>(f.mv, d.col, d.binom, np1, c);
         Mask<W> nx;
         if (mask_hits<W, K>(f.V, c)) {
             Mask<W> mid = f.V;
@@ -286,7 +308,7 @@ __device__ int node2_min_p3(const V2Dev& d, const int (&c2)[K], const Mask<W>& V
     int best = kV2None;
     for (int t = 0; t < mv.T; ++t) {
         int c[K];
-        const uint32_t cid = move_target<K>(mv, t, d.col, d.binom, np1, c);
+        const uint32_t cid = next_target<K>(mv, d.col, d.binom, np1, c);
         Mask<W> nx;
         if (mask_hits<W, K>(V2, c)) {
             Mask<W> mid = V2;
@@ -517,9 +539,11 @@ __global__ void __launch_bounds__(256) k_v2_root(V2Dev d) {
             int best = kV2None;
             Mask<W> nr;
             if (live) load_nbr<W>(nr, snbr, d.rwp, r);
+#pragma unroll
+            for (int i = 0; i < K; ++i) mv.idx[i] = 0;
             for (int t = 0; t < mv.T; ++t) {
                 int c1[K];
-                const uint32_t cid1 = move_target<K>(mv, t, d.col, d.binom, np1, c1);
+                const uint32_t cid1 = next_target<K>(mv, d.col, d.binom, np1, c1);
                 if (!live) continue;
                 bool rin = false;
 #pragma unroll
@@ -591,7 +615,7 @@ __global__ void k_v2_dilate(const uint8_t* __restrict__ in, uint8_t* out, const 
         uint8_t any = 0;
         for (int t = 0; t < mv.T && !any; ++t) {
             int cc[K];
-            const uint32_t s = move_target<K>(mv, t, adj, B, np1, cc);
+            const uint32_t s = next_target<K>(mv, adj, B, np1, cc);
             any = s < C ? in[s] : 0;
         }
         out[c] = any ? 1 : 0;

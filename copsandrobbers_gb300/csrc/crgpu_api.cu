@@ -636,6 +636,10 @@ static int v1_init_pass1(cr_solver* s, uint64_t* found) {
     CR_CUDA(ctx, cudaMemcpyAsync(s->d_meta, meta, sizeof(meta), cudaMemcpyHostToDevice, st));
     V1Dev d = dev_view(s);
     CR_CUDA(ctx, cudaEventRecord(s->evc0, st));
+    // the flag planes: every column-0 row holds captures (flag 1); column 1's flags are set by
+    // the kernel for the few rows that gain marks
+    CR_CUDA(ctx, cudaMemsetAsync(s->d_fflag, 1, s->C, st));
+    CR_CUDA(ctx, cudaMemsetAsync(s->d_fflag + s->C, 0, s->C, st));
     launch_init_pass1(d, s->grid_cop, st);
     CR_CUDA(ctx, cudaGetLastError());
     CR_CUDA(ctx, cudaEventRecord(s->evc1, st));

@@ -253,8 +253,9 @@ __device__ __forceinline__ void next_multiset(int (&c)[K], int n) {
 // keeps the masks of all cops but the last (they change once per n - c[k-2] steps).  Lane l
 // owns robbers 8l .. 8l+7 of each 256-vertex block, i.e. one 16-byte piece of the row, and
 // the 8-bit pieces of the marked and frontier rows, which four lanes assemble into a word.
-// The caller sets meta[0] = {0, 0, 0, 0, C, 0}, meta[1] = {1, empty, -1, 0, 0, 0} and zeroes
-// the pass counter; the pass counter then holds the first pass's count.
+// The caller sets meta[0] = {0, 0, 0, 0, C, 0}, meta[1] = {1, empty, -1, 0, 0, 0}, every
+// column-0 flag to 1 and every column-1 flag to 0, and zeroes the pass counter; the pass
+// counter then holds the first pass's count.
 // The same sweep for rows of one 256-robber block whose robbers split into whole lane pieces
 // (n <= 256, n a multiple of 8), arranged around the common case.  Column 0's marks are
 // cops | N(cops): lane l's word of them is the OR of the cops' neighbour words (its word index
@@ -304,10 +305,8 @@ __device__ CR_BODY_INLINE void init_pass1_single(const V1Dev& d, unsigned wk, un
     uint32_t* m1row = d.marked + ((size_t)d.C + cb) * rwp;
     const int frow_words = S * rwp;
     uint32_t* frow = d.front + ((size_t)d.C + cb) * frow_words;
-    uint8_t* fl0 = d.fflag + cb;
     uint8_t* fl1 = d.fflag + (size_t)d.C + cb;
-    for (size_t cid = cb; cid < ce; ++cid, trow += 2 * n, m0row += rwp, m1row += rwp, frow += frow_words,
-                ++fl0, ++fl1) {
+    for (size_t cid = cb; cid < ce; ++cid, trow += 2 * n, m0row += rwp, m1row += rwp, frow += frow_words, ++fl1) {
         if (cid > cb) next_multiset<K>(c, n);
         const int cl = c[K - 1];
         bool same = true;
@@ -417,10 +416,9 @@ __device__ CR_BODY_INLINE void init_pass1_single(const V1Dev& d, unsigned wk, un
             }
             for (int e = 2 * rwp + lane; e < frow_words; e += 32) frow[e] = 0u;
         }
-        if (lane == 0) {
-            *fl0 = 1;
-            *fl1 = changed ? 1 : 0;
-            rows1 += changed ? 1u : 0u;
+        if (lane == 0 && changed) {   // the caller set every column-0 flag and cleared column 1's
+            *fl1 = 1;
+            ++rows1;
         }
     }
     cnt = __reduce_add_sync(FULL_MASK, cnt);

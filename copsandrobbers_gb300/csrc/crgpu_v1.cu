@@ -76,8 +76,10 @@ template <int G>
 __global__ void __launch_bounds__(256) k_direct(V1Dev d, int col, int nx) {
     direct_body<G>(d, col, nx, blockIdx.x, gridDim.x);
 }
+// at most 64 registers: the grid runs 4 blocks of 256 per SM (more registers cost occupancy
+// that this latency-bound body needs more)
 template <bool P1, int G>
-__global__ void __launch_bounds__(256) k_and(V1Dev d, int col) {
+__global__ void __launch_bounds__(256, 4) k_and(V1Dev d, int col) {
     and_body<P1, G>(d, col, blockIdx.x, gridDim.x);
 }
 __global__ void k_verdict(const uint8_t* __restrict__ table, const uint32_t* __restrict__ m0,

@@ -52,12 +52,14 @@ template <int K, int NWP, int G>
 __global__ void __launch_bounds__(256) k_cop_pull(V1Dev d, int col, int nx) {
     cop_pull_body<K, NWP, G>(d, col, nx, blockIdx.x, gridDim.x);
 }
+// The separable cop turn is latency-bound too: at most 64 registers (4 blocks of 256 per SM),
+// or 80 (3 blocks) for 32-word rows, whose accumulators do not fit in 64 without spilling.
 template <int NWP, int G>
-__global__ void __launch_bounds__(256) k_pair_h1(V1Dev d, int nx) {
+__global__ void __launch_bounds__(256, NWP >= 32 ? 3 : 4) k_pair_h1(V1Dev d, int nx) {
     pair_h1_body<NWP, G>(d, nx, blockIdx.x, gridDim.x);
 }
 template <int NWP, int G>
-__global__ void __launch_bounds__(256) k_sep_pull(V1Dev d, int col, int nx) {
+__global__ void __launch_bounds__(256, NWP >= 32 ? 3 : 4) k_sep_pull(V1Dev d, int col, int nx) {
     sep_pull_body<NWP, G>(d, col, nx, blockIdx.x, gridDim.x);
 }
 template <int K, int G>

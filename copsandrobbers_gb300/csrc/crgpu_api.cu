@@ -108,7 +108,7 @@ struct cr_solver {
     // post-initializeCaptures state is read first
     bool init_pending = false;
     // small solves launch each pass's kernels directly: capturing and instantiating a graph
-    // costs more than it saves over a handful of short passes, and contends for the driver
+    // costs more than it saves over a handful of short passes, and contends for the CUDA driver
     // when many solves run side by side (the solve server)
     bool small = false;
     uint64_t base_caps = 0;

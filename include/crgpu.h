@@ -32,7 +32,7 @@ extern "C" {
 #define CR_ERR_INVALID 1   /* bad argument or malformed graph */
 #define CR_ERR_NOMEM 2     /* device memory exhausted or footprint admission refused */
 #define CR_ERR_CUDA 3      /* a CUDA runtime call failed */
-#define CR_ERR_LIMIT 4     /* size beyond what this build supports (n, k, config count) */
+#define CR_ERR_LIMIT 4     /* size beyond what the library supports (n, k, config count) */
 #define CR_ERR_INTERNAL 5  /* a device-side consistency check failed */
 #define CR_ERR_BUDGET 6    /* the pass budget ran out before the fixed point */
 #define CR_ERR_IO 7        /* file could not be read or written */

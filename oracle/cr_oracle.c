@@ -1,7 +1,7 @@
 /*
  * cr_oracle.c - CPU restatement of the reference k-cop solvers.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker for the GPU solver: the tests, the
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle the GPU solver is compared with: the tests, the
  * smoke check and the CPU-baseline leg of the benchmark call it.  No product code links it,
  * and the product never falls back to it.
  *

@@ -2,7 +2,8 @@
 
 Wraps ``libcroracle.so`` (the C restatement in ``cr_oracle.c``) and the reference binaries
 compiled into ``_ref/`` by ``build_ref.sh``.  Only the tests, ``__graft_entry__.smoke()`` and
-the CPU-baseline leg of ``bench.py`` import this module, and only as the checker.
+the CPU-baseline leg of ``bench.py`` import this module, and only as the oracle the GPU
+results are compared with.
 """
 from __future__ import annotations
 

@@ -1557,14 +1557,18 @@ __device__ CR_BODY_INLINE void and_body(const V1Dev& d, int col, unsigned wk, un
     t.flush(d, col, L.lane);
 }
 
-// findFinalResult (k_cops_visibility.cpp:301-331): key = worst << 32 | cid, minimised, is the
-// first config (lowest id) among those with the strictly smallest worst case.  Each lane
-// tests one config's column-0 row; the warp then scans the bytes of the complete rows.
+// findFinalResult (k_cops_visibility.cpp:301-331): over the configurations whose column-0 row
+// is all marked, the smallest (worst capture round, config id) key.  A warp takes 32
+// configurations at a time, each lane testing its own row's marks; the warp then reads each
+// full row (two columns: one 16-byte load per lane covers 8 robbers, 256 per step) and keeps a
+// per-lane running minimum, reduced once per warp into one atomic.
 __device__ CR_BODY_INLINE void verdict_body(const uint8_t* table, const uint32_t* m0, uint32_t C,
                                              int n, int rw, int rwp, int cols,
                                              unsigned long long* best, unsigned wk, unsigned nwk) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const size_t stride = (size_t)nwk * blockDim.x;
+    const bool vec = cols == 2 && (n & 7) == 0 && ((uintptr_t)table & 15u) == 0;
+    unsigned long long mine = ~0ull;
     for (size_t base = (size_t)wk * blockDim.x + warp * 32; base < C; base += stride) {
         const size_t cid = base + lane;
         bool full = cid < C;
@@ -1573,12 +1577,26 @@ __device__ CR_BODY_INLINE void verdict_body(const uint8_t* table, const uint32_t
         while (act) {
             const size_t c = base + __ffs(act) - 1;
             act &= act - 1;
-            int wc = 0;
-            for (int r = lane; r < n; r += 32) wc = max(wc, (int)(table[(c * n + r) * cols] >> 1));
+            const uint8_t* row = table + c * n * cols;
+            uint32_t wc = 0;
+            if (vec) {
+                for (int r0 = lane * 8; r0 < n; r0 += 256) {
+                    const uint4 v = *reinterpret_cast<const uint4*>(row + r0 * 2);
+                    // column-0 bytes are the even bytes; round = byte >> 1
+                    const uint32_t e0 = __byte_perm(v.x, v.y, 0x6420), e1 = __byte_perm(v.z, v.w, 0x6420);
+                    const uint32_t m = __vmaxu4(e0 >> 1 & 0x7F7F7F7Fu, e1 >> 1 & 0x7F7F7F7Fu);
+                    wc = max(wc, max(max(m & 0xFFu, (m >> 8) & 0xFFu), max((m >> 16) & 0xFFu, m >> 24)));
+                }
+            } else {
+                for (int r = lane; r < n; r += 32) wc = max(wc, (uint32_t)(row[(size_t)r * cols] >> 1));
+            }
             wc = __reduce_max_sync(FULL_MASK, wc);
-            if (lane == 0) atomicMin(best, ((unsigned long long)wc << 32) | c);
+            const unsigned long long key = ((unsigned long long)wc << 32) | c;
+            mine = key < mine ? key : mine;
         }
     }
+    // every lane holds the same running minimum (the keys are warp-uniform)
+    if (lane == 0 && mine != ~0ull) atomicMin(best, mine);
 }
 
 }  // namespace CR_BODY_NS

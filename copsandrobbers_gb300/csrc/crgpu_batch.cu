@@ -124,7 +124,9 @@ __host__ __device__ inline JobLayout job_layout(int n, int k, int p, int S) {
 __device__ inline uint64_t digest_word(const uint8_t* t, size_t bytes, size_t j) {
     uint64_t w = 0;
     const size_t at = j * 8;
-    if (at + 8 <= bytes) {
+    if (at + 8 <= bytes && ((uintptr_t)t & 7u) == 0) {
+        w = *reinterpret_cast<const uint64_t*>(t + at);   // little-endian: byte b at bits 8b
+    } else if (at + 8 <= bytes) {
         for (int b = 0; b < 8; ++b) w |= (uint64_t)t[at + b] << (8 * b);
     } else {
         for (size_t b = 0; at + b < bytes; ++b) w |= (uint64_t)t[at + b] << (8 * b);

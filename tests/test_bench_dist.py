@@ -57,3 +57,23 @@ def test_reference_arm_other_ranks_exit_quietly():
                         "--steps", "1", "--warmup", "0"], env=env, capture_output=True, text=True, timeout=120)
     assert r.returncode == 0
     assert r.stdout.strip() == ""
+
+
+def test_reference_arm_json_line():
+    """The reference arm's line (rank 0): the same metric and workload as the GPU arm, the
+    reference's CPU path timed on all host cores, an e2e equal to its own value."""
+    import json
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
+                        "--steps", "1", "--warmup", "0"], capture_output=True, text=True, timeout=600,
+                       env=dict(os.environ, RANK="0", WORLD_SIZE="1", LOCAL_RANK="0"))
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference"
+    assert line["metric"] == "resolved states/s" and line["unit"] == "states/s"
+    assert line["value"] > 0 and line["higher_is_better"] is True
+    assert line["steps"] == 1 and line["warmup"] == 0 and line["n_gpus"] == 1
+    assert "n=256" in line["config"]["workload"] and line["config"]["k"] == 3
+    cb = line["cpu_baseline"]
+    assert cb["value"] == line["value"] and cb["cores"] >= 1 and cb["kind"] in ("port", "reference")
+    assert line["e2e"] == {"value": line["value"], "unit": "states/s", "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}

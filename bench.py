@@ -200,6 +200,7 @@ def batched_workload(ctx, count: int = 4096, plain_sample: int = 128) -> dict:
             "batched_states_per_s": batched, "plain_states_per_s": plain,
             "batched_over_plain": batched / plain, "batched_ms": out.stats.ms,
             "states": int(out.stats.states), "ctas": int(out.stats.ctas), "threads": int(out.stats.threads),
+            "busy_frac": float(out.stats.busy_frac), "tail_ms": float(out.stats.tail_ms),
             "plain_sample_graphs": len(sample), "table_mismatches": mismatch,
             "cop_number_histogram": [int(x) for x in np.bincount(out.cop_numbers, minlength=4)]}
 

@@ -684,14 +684,28 @@ int v2_set_hash_capacity(V2Solver* s, uint64_t slots, std::string* err) {
     s->hkey = nullptr;
     s->hmask = nullptr;
     s->hval = nullptr;
+    s->hcap = 0;
+    s->chunk_nodes = 0;
+    s->hstats.capacity = 0;
+    if (!cap) return CR_OK;
+    // all three arrays or none: a solver whose table could not be allocated keeps working
+    // without one (every depth-2 node evaluated where it is reached)
+    cudaError_t e = cudaMalloc(&s->hkey, cap * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&s->hmask, cap * s->rwp * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&s->hval, cap);
+    if (e != cudaSuccess) {
+        void* got[] = {s->hkey, s->hmask, s->hval};
+        for (void* q : got)
+            if (q) cudaFree(q);
+        s->hkey = nullptr;
+        s->hmask = nullptr;
+        s->hval = nullptr;
+        if (err) *err = std::string("v2 cloud table: ") + cudaGetErrorString(e);
+        return e == cudaErrorMemoryAllocation ? CR_ERR_NOMEM : CR_ERR_CUDA;
+    }
     s->hcap = cap;
     s->chunk_nodes = cap / 2;
     s->hstats.capacity = cap;
-    if (cap) {
-        V2_CUDA(cudaMalloc(&s->hkey, cap * sizeof(unsigned long long)));
-        V2_CUDA(cudaMalloc(&s->hmask, cap * s->rwp * sizeof(uint32_t)));
-        V2_CUDA(cudaMalloc(&s->hval, cap));
-    }
     return CR_OK;
 }
 

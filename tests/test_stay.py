@@ -30,3 +30,30 @@ def test_oracle_stay_rules_match_legacy_solver(case):
     assert (cid >= 0) == (case["result"] == "WIN")
     if cid >= 0:
         assert [int(x) for x in sol.configs[cid]] == case["start"]
+
+
+LEGACY = os.path.join(os.path.dirname(GOLDEN), "..", "oracle", "_ref", "k_cops_4")
+
+
+@pytest.mark.skipif(not os.path.exists(LEGACY), reason="legacy reference solver not built")
+@pytest.mark.parametrize("i", range(16))
+def test_oracle_stay_rules_match_legacy_solver_live(tmp_path, i):
+    """The same check, live, on freshly generated seeded graphs."""
+    import re
+    import subprocess
+    rng = np.random.default_rng(900 + i)
+    n = int(rng.integers(8, 24))
+    kind = i % 3
+    g = (G.erdos_renyi(n, float(rng.uniform(2.0, 4.5)), 900 + i) if kind == 0 else
+         G.regular4(n + n % 2, 900 + i) if kind == 1 else G.delaunay_thinned(n, 900 + i))
+    k = int(rng.integers(1, 4 if g.n <= 16 else 3))
+    path = tmp_path / "g.txt"
+    G.save_matrix(g, path)
+    out = subprocess.run([LEGACY, str(path), str(k)], capture_output=True, text=True, timeout=300).stdout
+    result = re.search(r"RESULT: (WIN|LOSS)", out).group(1)
+    pos = re.search(r"Optimal Cop Start Positions: \(([^)]*)\)", out)
+    sol = O.solve_v1(g, k, 1, cop_stay=True, robber_stay=True)
+    cid = first_universal_win(sol)
+    assert (cid >= 0) == (result == "WIN")
+    if cid >= 0:
+        assert [int(x) for x in sol.configs[cid]] == [int(x) for x in pos.group(1).split(",")]

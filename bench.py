@@ -408,9 +408,16 @@ def run_gpu(args) -> None:
     line = None
     extra = {}
     if rank == 0 and not args.headline_only:
-        extra["batched"] = batched_workload(ctx)
-        extra["limited_visibility"] = limited_visibility_workload(ctx)
-        extra["serving"] = serving_workload(args.serving_requests, args.serving_rate)
+        # the other workloads of the benchmark; a failure in one is reported in its key and
+        # does not take the headline line with it
+        for key, run in (("batched", lambda: batched_workload(ctx)),
+                         ("limited_visibility", lambda: limited_visibility_workload(ctx)),
+                         ("serving", lambda: serving_workload(args.serving_requests, args.serving_rate))):
+            try:
+                extra[key] = run()
+            except Exception as e:  # noqa: BLE001 - reported, not swallowed
+                extra[key] = {"error": f"{type(e).__name__}: {e}"}
+                print(f"bench: {key} workload failed: {e}", file=sys.stderr, flush=True)
     if rank == 0:
         base = cpu_baseline(g, k, p, passes) if not args.no_cpu_baseline else None
         line = {

@@ -438,6 +438,16 @@ static int alloc_v1(cr_solver* s) {
                 for (uint32_t f = rrp[v]; f < rrp[v + 1]; ++f) m[(size_t)rcol[f] * npad + r] &= ~(1u << j);
             }
         }
+        // plane 0 as the first pass's fast test wants it: a cop's own entry [c][c] all ones (a
+        // robber on a cop is never a column-1 mark, so the entry's value is otherwise unused)
+        // and the rows of cops that cannot move zero (those rows are read only when every cop
+        // of the configuration can move)
+        const uint32_t ones = W == 4 ? 0xFFFFFFFFu : ((1u << (8 * W)) - 1u);
+        for (int c = 0; c < n; ++c) {
+            m[(size_t)c * npad + c] = ones;
+            if (crp[c + 1] == crp[c])
+                for (int r = 0; r < npad; ++r) m[(size_t)c * npad + r] = 0u;
+        }
         std::vector<uint8_t> bytes(m.size() * W);
         for (size_t i = 0; i < m.size(); ++i)
             for (int b = 0; b < W; ++b) bytes[i * W + b] = (uint8_t)(m[i] >> (8 * b));

@@ -55,7 +55,9 @@ struct DevGraph {
     const uint32_t* rhop;     // [n][rwp]: bit r of row u set iff u is in hop(r) (transposed hop)
     // Uncovered-slot masks for the first pass's closed form (cover_w bytes per mask, 0 = not
     // built; npad = n rounded up to 8).  Bit j of a mask refers to r's j-th out-neighbour:
-    //   cover[c][r]            bit j set iff that neighbour is neither c nor an out-neighbour of c
+    //   cover[c][r]            bit j set iff that neighbour is neither c nor an out-neighbour of c;
+    //                          except cover[c][c] = all ones and, for a cop c without a move,
+    //                          cover[c][*] = 0 (read only when every cop can move)
     //   cover[n + c][r]        bit j set iff that neighbour is not c
     const uint8_t* cover;
     int cover_w;

@@ -45,8 +45,14 @@ using namespace grid;
 
 __global__ void k_prep(V1Dev d, int col, int nx) { prep_body(d, col, nx, blockIdx.x, gridDim.x); }
 __global__ void k_init(V1Dev d, int K) { init_body(d, K, blockIdx.x, gridDim.x); }
-template <int K, int W>
-__global__ void __launch_bounds__(256) k_init_pass1(V1Dev d) { init_pass1_body<K, W>(d, blockIdx.x, gridDim.x); }
+// The first pass in two instances: rows of one 256-robber block split into whole lane pieces
+// (the run form), and every other row shape.  At most 64 registers: 4 blocks of 256 per SM
+// keep enough stores in flight.
+template <int K, int W, bool SINGLE>
+__global__ void __launch_bounds__(256, 4) k_init_pass1(V1Dev d) {
+    if (SINGLE) init_pass1_single<K, W>(d, blockIdx.x, gridDim.x);
+    else init_pass1_body<K, W>(d, blockIdx.x, gridDim.x);
+}
 
 template <int K, int NWP, int G>
 __global__ void __launch_bounds__(256) k_cop_pull(V1Dev d, int col, int nx) {
@@ -272,22 +278,28 @@ void launch_prep(const V1Dev& d, int col, int nx, int grid, cudaStream_t st) {
 
 void launch_init(const V1Dev& d, int grid, cudaStream_t st) { k_init<<<grid, 256, 0, st>>>(d, d.k); }
 
-template <int W>
+template <int W, bool SINGLE>
 static void launch_init_pass1_w(const V1Dev& d, int grid, size_t sm, cudaStream_t st) {
     switch (d.k) {
-        case 1: k_init_pass1<1, W><<<grid, 256, sm, st>>>(d); break;
-        case 2: k_init_pass1<2, W><<<grid, 256, sm, st>>>(d); break;
-        case 3: k_init_pass1<3, W><<<grid, 256, sm, st>>>(d); break;
-        default: k_init_pass1<4, W><<<grid, 256, sm, st>>>(d); break;
+        case 1: k_init_pass1<1, W, SINGLE><<<grid, 256, sm, st>>>(d); break;
+        case 2: k_init_pass1<2, W, SINGLE><<<grid, 256, sm, st>>>(d); break;
+        case 3: k_init_pass1<3, W, SINGLE><<<grid, 256, sm, st>>>(d); break;
+        default: k_init_pass1<4, W, SINGLE><<<grid, 256, sm, st>>>(d); break;
     }
 }
+template <bool SINGLE>
+static void launch_init_pass1_s(const V1Dev& d, int grid, size_t sm, cudaStream_t st) {
+    if (d.g.cover_w == 1) launch_init_pass1_w<1, SINGLE>(d, grid, sm, st);
+    else if (d.g.cover_w == 2) launch_init_pass1_w<2, SINGLE>(d, grid, sm, st);
+    else launch_init_pass1_w<4, SINGLE>(d, grid, sm, st);
+}
 
-// Requires d.g.cover (cover_w 1, 2 or 4) and two columns.
+// Requires d.g.cover (cover_w 1, 2 or 4) and two columns.  Rows of one 256-robber block
+// split into whole lane pieces take the run form, which needs its tables in shared memory.
 void launch_init_pass1(const V1Dev& d, int grid, cudaStream_t st) {
-    const size_t sm = 0;
-    if (d.g.cover_w == 1) launch_init_pass1_w<1>(d, grid, sm, st);
-    else if (d.g.cover_w == 2) launch_init_pass1_w<2>(d, grid, sm, st);
-    else launch_init_pass1_w<4>(d, grid, sm, st);
+    const bool single = d.g.n <= 256 && (d.g.n & 7) == 0;
+    if (single) launch_init_pass1_s<true>(d, grid, (size_t)init_pass1_smem_words(d.g.n, d.g.rwp) * 4, st);
+    else launch_init_pass1_s<false>(d, grid, 0, st);
 }
 
 void launch_verdict(const V1Dev& d, int cols, unsigned long long* best, int grid, cudaStream_t st) {

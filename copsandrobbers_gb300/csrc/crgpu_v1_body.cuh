@@ -191,6 +191,21 @@ struct Cov8 {
 #pragma unroll
         for (int q = 0; q < NW; ++q) w[q] &= o.w[q];
     }
+    // some robber's mask is zero (the exact zero-byte / zero-halfword tests)
+    __device__ __forceinline__ bool has_zero() const {
+        uint32_t t = 0;
+        if (W == 1) {
+#pragma unroll
+            for (int q = 0; q < 2; ++q) t |= (w[q] - 0x01010101u) & ~w[q] & 0x80808080u;
+        } else if (W == 2) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) t |= (w[q] - 0x00010001u) & ~w[q] & 0x80008000u;
+        } else {
+#pragma unroll
+            for (int q = 0; q < 8; ++q) t |= w[q] == 0u ? 1u : 0u;
+        }
+        return t != 0u;
+    }
     // bit j set iff robber j's mask is zero
     __device__ __forceinline__ uint32_t zero_bits() const {
         uint32_t b = 0;
@@ -257,15 +272,31 @@ __device__ __forceinline__ void next_multiset(int (&c)[K], int n) {
 // column-0 flag to 1 and every column-1 flag to 0, and zeroes the pass counter; the pass
 // counter then holds the first pass's count.
 // The same sweep for rows of one 256-robber block whose robbers split into whole lane pieces
-// (n <= 256, n a multiple of 8), arranged around the common case.  Column 0's marks are
-// cops | N(cops): lane l's word of them is the OR of the cops' neighbour words (its word index
-// is l / 4), so the marked rows need no shuffles.  Column 1 gains marks only where N(r) lies
-// in M0, which on most graphs happens for few configurations: only when some lane of the warp
-// has such a robber does the warp split those marks by round, patch their bytes and assemble
-// the frontier words.  Cop bytes (0x01 in both columns) are patched by a uniform loop over
-// the K cops.  Results are byte-identical to the general sweep.
+// (n <= 256, n a multiple of 8), organised around the common configuration.  Consecutive
+// configurations share their leading cops c[0 .. K-2] for a run of up to n of them (only the
+// last cop moves on), so the sweep is a loop over runs and, inside, over the last cop.  What
+// depends on the leading cops is set up once per run: the AND of their uncovered-slot masks,
+// their neighbour word (column 0's marks are cops | N(cops)), their bits among the lane's
+// robbers, and the 16-byte XOR patch that turns those robbers' bytes into 0x01 0x01.
+// Per configuration the warp tests whether some robber of a lane is left with no uncovered slot
+// (a zero mask after ANDing the last cop's cover row: one 8-byte load and a zero-byte test).
+// The cover table is built so that this test also catches everything else the fast form does
+// not handle: a cop's own entry cover[c][c] is all ones (a robber on a cop is a capture, never a
+// column-1 mark, so the entry's value is otherwise irrelevant), and the rows of cops that cannot
+// move are zero.  When no lane trips and every leading cop can move (nearly always), column 1
+// gains no mark and the configuration takes the fast form: the lane's 16-byte piece is a
+// shared-memory table entry indexed by its 8 column-0 seed bits, XORed with the leading cops'
+// patch and stored once; the last cop's two bytes follow as one 2-byte store; one store per
+// row word writes the marked words; nothing else is written (the column-1 frontier row and flag
+// stay as the caller cleared them).  Otherwise it takes the general form, which tests every
+// robber exactly, splits its column-1 marks by round, patches their bytes and writes the
+// frontier words.  Results are byte-identical to the general sweep.  Dynamic shared memory:
+// init_pass1_smem_words(n, rwp) words.
+__host__ __device__ inline int init_pass1_smem_words(int n, int rwp) { return 256 * 4 + n * rwp; }
+
 template <int K, int W>
 __device__ CR_BODY_INLINE void init_pass1_single(const V1Dev& d, unsigned wk, unsigned nwk) {
+    extern __shared__ uint32_t sm[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int n = d.g.n, rw = d.g.rw, rwp = d.g.rwp, S = d.S, npad = d.g.npad;
     const uint32_t* CR_RESTRICT nbr = d.g.nbr;
@@ -273,7 +304,20 @@ __device__ CR_BODY_INLINE void init_pass1_single(const V1Dev& d, unsigned wk, un
     const uint8_t* CR_RESTRICT cover = d.g.cover;
     const size_t plane = (size_t)n * npad * W;
     const bool padded = rw != rwp || S > 2;
-    unsigned cnt = 0, rows1 = 0, any_seed = 0, any1 = 0, any2 = 0;
+    // shared memory: the piece table (entry s: robbers j with bit j of s set read 0x03 in
+    // column 0, every other byte 0xFE) and the cops' neighbour rows
+    uint4* lut = reinterpret_cast<uint4*>(sm);
+    uint32_t* snbr = sm + 256 * 4;
+    for (int t = threadIdx.x; t < 256; t += blockDim.x) {
+        const uint32_t s0 = 0xFEFEFEFEu ^ (nibble_bytes(t & 0xF) & 0xFDFDFDFDu);
+        const uint32_t s1 = 0xFEFEFEFEu ^ (nibble_bytes(t >> 4) & 0xFDFDFDFDu);
+        const uint32_t fe = 0xFEFEFEFEu;
+        lut[t] = make_uint4(__byte_perm(s0, fe, 0x5140), __byte_perm(s0, fe, 0x7362),
+                            __byte_perm(s1, fe, 0x5140), __byte_perm(s1, fe, 0x7362));
+    }
+    for (int t = threadIdx.x; t < n * rwp; t += blockDim.x) snbr[t] = CR_LDG(&nbr[t]);
+    __syncthreads();
+    unsigned cnt = 0, cnt1 = 0, rows1 = 0, any1 = 0, any2 = 0;
     const size_t nwarps = (size_t)nwk * (blockDim.x >> 5);
     const size_t chunk = (d.C + nwarps - 1) / nwarps;
     const size_t cb = ((size_t)wk * (blockDim.x >> 5) + warp) * chunk;
@@ -289,147 +333,181 @@ __device__ CR_BODY_INLINE void init_pass1_single(const V1Dev& d, unsigned wk, un
     const int sh = (lane & 3) * 8;            // and their bit offset in it
     const uint32_t lvalid = live ? 0xFFu : 0u;
     const bool writer = (lane & 3) == 0 && wi < rw;
-    // the cops c[0 .. K-2], kept while they stay put: the AND of their uncovered masks (with
-    // and without their neighbourhoods), whether all can move, their neighbour word, and their
-    // bits among this lane's robbers and in its word
-    int pre[K > 1 ? K - 1 : 1];
+    // fast form: lane 4w writes word w of the column-0 marked row, lane 4w + 1 that of column 1
+    const bool mwriter = (lane & 3) < 2 && wi < rw;
+    const size_t mplane = (lane & 1) ? (size_t)d.C * rwp : 0;
+    size_t cid = cb;
+    while (cid < ce) {
+        // a new run of the leading cops c[0 .. K-2]: the AND of their uncovered masks (with and
+        // without their neighbourhoods), whether all can move, their neighbour word, their bits
+        // among this lane's robbers and in its word, and the XOR patch of their bytes
+        Cov8<W> zpre, znpre;
+        zpre.ones();
+        znpre.ones();
+        bool mpre = true;
+        uint32_t npre = 0, cpre = 0, cpw = 0;
 #pragma unroll
-    for (int i = 0; i < K - 1; ++i) pre[i] = -1;
-    Cov8<W> zpre, znpre;
-    zpre.ones();
-    znpre.ones();
-    bool mpre = true;
-    uint32_t npre = 0, cpre = 0, cpw = 0;
-    uint8_t* trow = d.table + cb * n * 2;
-    uint32_t* m0row = d.marked + cb * rwp;
-    uint32_t* m1row = d.marked + ((size_t)d.C + cb) * rwp;
-    const int frow_words = S * rwp;
-    uint32_t* frow = d.front + ((size_t)d.C + cb) * frow_words;
-    uint8_t* fl1 = d.fflag + (size_t)d.C + cb;
-    for (size_t cid = cb; cid < ce; ++cid, trow += 2 * n, m0row += rwp, m1row += rwp, frow += frow_words, ++fl1) {
-        if (cid > cb) next_multiset<K>(c, n);
-        const int cl = c[K - 1];
-        bool same = true;
-#pragma unroll
-        for (int i = 0; i < K - 1; ++i) same &= pre[i] == c[i];
-        if (!same) {
-            zpre.ones();
-            znpre.ones();
-            mpre = true;
-            npre = 0;
-            cpre = 0;
-            cpw = 0;
-#pragma unroll
-            for (int i = 0; i < K - 1; ++i) {
-                pre[i] = c[i];
-                mpre &= !((CR_LDG(&iso[c[i] >> 5]) >> (c[i] & 31)) & 1u);
-                if ((c[i] >> 5) == wi) cpw |= 1u << (c[i] & 31);
+        for (int i = 0; i < K - 1; ++i) {
+            mpre &= !((CR_LDG(&iso[c[i] >> 5]) >> (c[i] & 31)) & 1u);
+            if ((c[i] >> 5) == wi) cpw |= 1u << (c[i] & 31);
+            if (live) {
+                npre |= snbr[c[i] * rwp + wi];
+                const unsigned dv = (unsigned)(c[i] - lr0);
+                if (dv < 8u) cpre |= 1u << dv;
+                Cov8<W> t;
+                t.load(cover + (uint32_t)(c[i] * npad + lr0) * W);
+                zpre.andd(t);
+                t.load(cover + plane + (uint32_t)(c[i] * npad + lr0) * W);
+                znpre.andd(t);
+            }
+        }
+        uint4 capx;
+        capx.x = ((cpre & 1u) ? 0x0000FFFFu : 0u) | ((cpre & 2u) ? 0xFFFF0000u : 0u);
+        capx.y = ((cpre & 4u) ? 0x0000FFFFu : 0u) | ((cpre & 8u) ? 0xFFFF0000u : 0u);
+        capx.z = ((cpre & 16u) ? 0x0000FFFFu : 0u) | ((cpre & 32u) ? 0xFFFF0000u : 0u);
+        capx.w = ((cpre & 64u) ? 0x0000FFFFu : 0u) | ((cpre & 128u) ? 0xFFFF0000u : 0u);
+        int cl = c[K - 1];
+        const size_t run_end = cid + (size_t)(n - cl) < ce ? cid + (size_t)(n - cl) : ce;
+        uint8_t* dst = d.table + cid * n * 2 + lr0 * 2;
+        uint32_t* mrow = d.marked + mplane + cid * rwp + wi;
+        const uint8_t* cv = cover + (size_t)(cl * npad + lr0) * W;
+        for (; cid < run_end; ++cid, ++cl, dst += 2 * n, mrow += rwp, cv += (size_t)npad * W) {
+            const unsigned dl = (unsigned)(cl - lr0);
+            const uint32_t capb = cpre | (dl < 8u ? 1u << dl : 0u);
+            const uint32_t capw = cpw | ((cl >> 5) == wi ? 1u << (cl & 31) : 0u);
+            bool trip = false;
+            if (live) {
+                Cov8<W> z;
+                z.load(cv);
+                z.andd(zpre);
+                trip = z.has_zero();
+            }
+            if (!__any_sync(FULL_MASK, trip) && mpre) {
+                // fast form: every cop can move and column 1 gains no mark
+                const uint32_t xw = live ? (npre | snbr[cl * rwp + wi]) : 0u;
+                const uint32_t seedb = (xw >> sh) & 0xFFu & ~capb;
                 if (live) {
-                    npre |= CR_LDG(&nbr[c[i] * rwp + wi]);
-                    const unsigned dv = (unsigned)(c[i] - lr0);
-                    if (dv < 8u) cpre |= 1u << dv;
-                    Cov8<W> t;
-                    t.load(cover + (uint32_t)(c[i] * npad + lr0) * W);
-                    zpre.andd(t);
-                    t.load(cover + plane + (uint32_t)(c[i] * npad + lr0) * W);
-                    znpre.andd(t);
+                    uint4 pc = lut[seedb];
+                    pc.x ^= capx.x;
+                    pc.y ^= capx.y;
+                    pc.z ^= capx.z;
+                    pc.w ^= capx.w;
+                    *reinterpret_cast<uint4*>(dst) = pc;
+                    if (dl < 8u) *reinterpret_cast<uint16_t*>(dst + 2 * dl) = 0x0101u;
+                }
+                cnt += __popc(seedb);
+                if (mwriter) *mrow = (lane & 1) ? capw : (xw | capw);
+                if (padded) {
+                    uint32_t* m0row = d.marked + cid * rwp;
+                    uint32_t* m1row = d.marked + ((size_t)d.C + cid) * rwp;
+                    for (int e = rw + lane; e < rwp; e += 32) {
+                        m0row[e] = 0u;
+                        m1row[e] = 0u;
+                    }
+                }
+                continue;
+            }
+            // general form
+            const bool moves = mpre && !((CR_LDG(&iso[cl >> 5]) >> (cl & 31)) & 1u);
+            const uint32_t off = (uint32_t)(cl * npad + lr0) * W;
+            uint32_t xw = 0, a = 0;
+            if (live) {
+                // N(r) within M0 iff no slot of r stays uncovered (M0 = the cops alone when
+                // some cop cannot move)
+                Cov8<W> z = moves ? zpre : znpre, t;
+                t.load(cover + (moves ? 0 : plane) + off);
+                z.andd(t);
+                a = z.zero_bits() & ~capb & lvalid;
+                if (moves) xw = npre | snbr[cl * rwp + wi];
+            }
+            const uint32_t seedb = (xw >> sh) & 0xFFu & ~capb;
+            if (live) {
+                uint4 pc = lut[seedb];
+                pc.x ^= capx.x;
+                pc.y ^= capx.y;
+                pc.z ^= capx.z;
+                pc.w ^= capx.w;
+                *reinterpret_cast<uint4*>(dst) = pc;
+                if (dl < 8u) *reinterpret_cast<uint16_t*>(dst + 2 * dl) = 0x0101u;
+            }
+            cnt += __popc(seedb);
+            uint32_t m1w = capw;
+            const bool changed = __any_sync(FULL_MASK, a != 0u);
+            if (changed) {
+                // column-1 marks: round 2 when some neighbour of r is not a cop, else round 1
+                uint32_t deepb = 0;
+                if (live) {
+                    Cov8<W> zn = znpre, t;
+                    t.load(cover + plane + off);
+                    zn.andd(t);
+                    deepb = ~zn.zero_bits();
+                }
+                const uint32_t a2 = a & deepb, a1 = a & ~deepb;
+                uint32_t sp = a;
+                while (sp) {
+                    const int j = __ffs(sp) - 1;
+                    sp &= sp - 1;
+                    const uint32_t bit = 1u << j;
+                    const uint32_t v0 = (seedb & bit) ? 0x03u : 0xFEu;
+                    const uint32_t v1 = (a1 & bit) ? 0x03u : 0x05u;
+                    *reinterpret_cast<uint16_t*>(dst + 2 * j) = (uint16_t)(v0 | (v1 << 8));
+                }
+                cnt1 += __popc(a1) + __popc(a2);
+                any1 |= a1;
+                any2 |= a2;
+                // the 8-bit pieces of lanes 4w .. 4w+3 make word w of the column-1 frontier slots
+                const uint32_t v = a1 | a2 << 8;
+                const uint32_t v1 = __shfl_down_sync(FULL_MASK, v, 1);
+                const uint32_t v2 = __shfl_down_sync(FULL_MASK, v, 2);
+                const uint32_t v3 = __shfl_down_sync(FULL_MASK, v, 3);
+                const uint32_t t01 = __byte_perm(v, v1, 0x5140), t23 = __byte_perm(v2, v3, 0x5140);
+                const uint32_t a1w = __byte_perm(t01, t23, 0x5410), a2w = __byte_perm(t01, t23, 0x7632);
+                m1w |= a1w | a2w;
+                uint32_t* frow = d.front + ((size_t)d.C + cid) * (size_t)(S * rwp);
+                if (writer) {
+                    frow[wi] = a1w;
+                    frow[rwp + wi] = a2w;
+                }
+                if (padded) {
+                    for (int e = rw + lane; e < rwp; e += 32) {
+                        frow[e] = 0u;
+                        frow[rwp + e] = 0u;
+                    }
+                    for (int e = 2 * rwp + lane; e < S * rwp; e += 32) frow[e] = 0u;
+                }
+                if (lane == 0) {   // the caller set every column-0 flag and cleared column 1's
+                    d.fflag[(size_t)d.C + cid] = 1;
+                    ++rows1;
+                }
+            }
+            uint32_t* m0row = d.marked + cid * rwp;
+            uint32_t* m1row = d.marked + ((size_t)d.C + cid) * rwp;
+            if (writer) {
+                m0row[wi] = xw | capw;
+                m1row[wi] = m1w;
+            }
+            if (padded) {
+                for (int e = rw + lane; e < rwp; e += 32) {
+                    m0row[e] = 0u;
+                    m1row[e] = 0u;
                 }
             }
         }
-        const bool moves = mpre && !((CR_LDG(&iso[cl >> 5]) >> (cl & 31)) & 1u);
-        const unsigned dl = (unsigned)(cl - lr0);
-        const uint32_t capb = cpre | (dl < 8u ? 1u << dl : 0u);
-        const uint32_t capw = cpw | ((cl >> 5) == wi ? 1u << (cl & 31) : 0u);
-        const uint32_t off = (uint32_t)(cl * npad + lr0) * W;
-        uint32_t xw = 0, a = 0;
-        if (live) {
-            // N(r) within M0 iff no slot of r stays uncovered (M0 = the cops alone when some
-            // cop cannot move)
-            Cov8<W> z = moves ? zpre : znpre, t;
-            t.load(cover + (moves ? 0 : plane) + off);
-            z.andd(t);
-            a = z.zero_bits() & ~capb & lvalid;
-            if (moves) xw = npre | CR_LDG(&nbr[cl * rwp + wi]);
-        }
-        const uint32_t seedb = (xw >> sh) & 0xFFu & ~capb;
-        uint8_t* dst = trow + lr0 * 2;
-        if (live) {
-            const uint32_t s0 = 0xFEFEFEFEu ^ (nibble_bytes(seedb & 0xFu) & 0xFDFDFDFDu);
-            const uint32_t s1 = 0xFEFEFEFEu ^ (nibble_bytes(seedb >> 4) & 0xFDFDFDFDu);
-            const uint32_t fe = 0xFEFEFEFEu;
-            *reinterpret_cast<uint4*>(dst) = make_uint4(__byte_perm(s0, fe, 0x5140), __byte_perm(s0, fe, 0x7362),
-                                                        __byte_perm(s1, fe, 0x5140), __byte_perm(s1, fe, 0x7362));
-        }
-        // a robber on a cop: round 0 in both columns (written after the piece, same thread)
-#pragma unroll
-        for (int i = 0; i < K; ++i)
-            if ((unsigned)(c[i] - lr0) < 8u) *reinterpret_cast<uint16_t*>(trow + 2 * c[i]) = 0x0101u;
-        cnt += __popc(seedb);
-        any_seed |= seedb;
-        uint32_t m1w = capw;
-        const bool changed = __any_sync(FULL_MASK, a != 0u);
-        if (changed) {
-            // column-1 marks: round 2 when some neighbour of r is not a cop, else round 1
-            uint32_t deepb = 0;
-            if (live) {
-                Cov8<W> zn = znpre, t;
-                t.load(cover + plane + off);
-                zn.andd(t);
-                deepb = ~zn.zero_bits();
-            }
-            const uint32_t a2 = a & deepb, a1 = a & ~deepb;
-            uint32_t sp = a;
-            while (sp) {
-                const int j = __ffs(sp) - 1;
-                sp &= sp - 1;
-                const uint32_t bit = 1u << j;
-                const uint32_t v0 = (seedb & bit) ? 0x03u : 0xFEu;
-                const uint32_t v1 = (a1 & bit) ? 0x03u : 0x05u;
-                *reinterpret_cast<uint16_t*>(dst + 2 * j) = (uint16_t)(v0 | (v1 << 8));
-            }
-            cnt += __popc(a1) + __popc(a2);
-            any1 |= a1;
-            any2 |= a2;
-            // the 8-bit pieces of lanes 4w .. 4w+3 make word w of the column-1 frontier slots
-            const uint32_t v = a1 | a2 << 8;
-            const uint32_t v1 = __shfl_down_sync(FULL_MASK, v, 1);
-            const uint32_t v2 = __shfl_down_sync(FULL_MASK, v, 2);
-            const uint32_t v3 = __shfl_down_sync(FULL_MASK, v, 3);
-            const uint32_t t01 = __byte_perm(v, v1, 0x5140), t23 = __byte_perm(v2, v3, 0x5140);
-            const uint32_t a1w = __byte_perm(t01, t23, 0x5410), a2w = __byte_perm(t01, t23, 0x7632);
-            m1w |= a1w | a2w;
-            if (writer) {
-                frow[wi] = a1w;
-                frow[rwp + wi] = a2w;
-            }
-        }
-        if (writer) {
-            m0row[wi] = xw | capw;
-            m1row[wi] = m1w;
-        }
-        if (padded) {
-            for (int e = rw + lane; e < rwp; e += 32) {
-                m0row[e] = 0u;
-                m1row[e] = 0u;
-                frow[e] = 0u;
-                frow[rwp + e] = 0u;
-            }
-            for (int e = 2 * rwp + lane; e < frow_words; e += 32) frow[e] = 0u;
-        }
-        if (lane == 0 && changed) {   // the caller set every column-0 flag and cleared column 1's
-            *fl1 = 1;
-            ++rows1;
+        // the run is over: step the multiset past its last configuration
+        if (cid < ce) {
+            c[K - 1] = n - 1;
+            next_multiset<K>(c, n);
         }
     }
-    cnt = __reduce_add_sync(FULL_MASK, cnt);
+    const unsigned seeds = __reduce_add_sync(FULL_MASK, cnt);
+    cnt1 = __reduce_add_sync(FULL_MASK, cnt1);
     rows1 = __reduce_add_sync(FULL_MASK, rows1);
-    any_seed = __reduce_or_sync(FULL_MASK, any_seed);
     any1 = __reduce_or_sync(FULL_MASK, any1);
     any2 = __reduce_or_sync(FULL_MASK, any2);
     if (lane == 0) {
-        if (cnt) atomicAdd(d.pass_new, (unsigned long long)cnt);
+        if (seeds + cnt1) atomicAdd(d.pass_new, (unsigned long long)(seeds + cnt1));
         if (rows1) atomicAdd(&d.meta[1].rows, (int)rows1);
-        if (any_seed) atomicMax(&d.meta[0].hi, 1);
+        if (seeds) atomicMax(&d.meta[0].hi, 1);
         if (any1 | any2) {
             atomicMin(&d.meta[1].lo, any1 ? 1 : 2);
             atomicMax(&d.meta[1].hi, any2 ? 2 : 1);
@@ -437,12 +515,10 @@ __device__ CR_BODY_INLINE void init_pass1_single(const V1Dev& d, unsigned wk, un
     }
 }
 
+// The general sweep (any row shape; the launcher sends single-block rows of whole lane pieces
+// to init_pass1_single).
 template <int K, int W>
 __device__ CR_BODY_INLINE void init_pass1_body(const V1Dev& d, unsigned wk, unsigned nwk) {
-    if (d.g.n <= 256 && (d.g.n & 7) == 0) {
-        init_pass1_single<K, W>(d, wk, nwk);
-        return;
-    }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int n = d.g.n, rw = d.g.rw, rwp = d.g.rwp, S = d.S, npad = d.g.npad;
     const uint32_t* CR_RESTRICT nbr = d.g.nbr;

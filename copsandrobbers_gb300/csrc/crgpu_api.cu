@@ -20,7 +20,7 @@ void launch_cop(const V1Dev& d, int col, int nx, int direct, int grid, cudaStrea
 void launch_and(const V1Dev& d, int col, bool p1, int grid, cudaStream_t st);
 void launch_prep(const V1Dev& d, int col, int nx, int grid, cudaStream_t st);
 void launch_init(const V1Dev& d, int grid, cudaStream_t st);
-void launch_init_pass1(const V1Dev& d, int grid, cudaStream_t st);
+void launch_init_pass1(const V1Dev& d, int num_sms, cudaStream_t st);
 void launch_marks_from_table(const uint8_t* table, uint32_t C, int n, int cols, int rwp, uint32_t* marked,
                              int grid, cudaStream_t st);
 void launch_game(const uint8_t* table, const uint16_t* configs, const unsigned long long* heads,
@@ -633,9 +633,9 @@ static int v1_init(cr_solver* s, uint64_t* caps) {
     return CR_OK;
 }
 
-// initializeCaptures and pass 1 of a p = 1 solve in one kernel (init_pass1_body): every table
-// byte, both marked planes, column 1's frontier and both flag planes are written whole, so
-// nothing is cleared first.
+// initializeCaptures and pass 1 of a p = 1 solve in one kernel (init_pass1_single /
+// init_pass1_body): every table byte, both marked planes and both flag planes are written whole
+// (column 1's frontier rows where they gained marks), so nothing is cleared first.
 static int v1_init_pass1(cr_solver* s, uint64_t* found) {
     cr_context* ctx = s->ctx;
     cudaStream_t st = ctx->stream;
@@ -646,11 +646,7 @@ static int v1_init_pass1(cr_solver* s, uint64_t* found) {
     CR_CUDA(ctx, cudaMemcpyAsync(s->d_meta, meta, sizeof(meta), cudaMemcpyHostToDevice, st));
     V1Dev d = dev_view(s);
     CR_CUDA(ctx, cudaEventRecord(s->evc0, st));
-    // the flag planes: every column-0 row holds captures (flag 1); column 1's flags are set by
-    // the kernel for the few rows that gain marks
-    CR_CUDA(ctx, cudaMemsetAsync(s->d_fflag, 1, s->C, st));
-    CR_CUDA(ctx, cudaMemsetAsync(s->d_fflag + s->C, 0, s->C, st));
-    launch_init_pass1(d, s->grid_cop, st);
+    launch_init_pass1(d, ctx->num_sms, st);
     CR_CUDA(ctx, cudaGetLastError());
     CR_CUDA(ctx, cudaEventRecord(s->evc1, st));
     CR_CUDA(ctx, cudaMemcpyAsync(s->h_pinned, s->d_counters, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));

@@ -33,6 +33,8 @@
 // the seed rows over T(C) is the union of the cops' neighbourhoods.
 #include "crgpu_internal.cuh"
 
+#include <algorithm>
+
 #define CR_BODY_NS grid
 #define CR_LDG(p) __ldg(p)
 #define CR_RESTRICT __restrict__
@@ -46,12 +48,16 @@ using namespace grid;
 __global__ void k_prep(V1Dev d, int col, int nx) { prep_body(d, col, nx, blockIdx.x, gridDim.x); }
 __global__ void k_init(V1Dev d, int K) { init_body(d, K, blockIdx.x, gridDim.x); }
 // The first pass in two instances: rows of one 256-robber block split into whole lane pieces
-// (the run form), and every other row shape.  At most 64 registers: 4 blocks of 256 per SM
-// keep enough stores in flight.
+// (the run form; at most 85 registers, 3 blocks of 256 per SM, which measured faster than 64
+// registers at 4 blocks and than 2 blocks), and every other row shape (64 registers).
 template <int K, int W, bool SINGLE>
-__global__ void __launch_bounds__(256, 4) k_init_pass1(V1Dev d) {
-    if (SINGLE) init_pass1_single<K, W>(d, blockIdx.x, gridDim.x);
-    else init_pass1_body<K, W>(d, blockIdx.x, gridDim.x);
+__global__ void __launch_bounds__(256, SINGLE ? 3 : 4) k_init_pass1(V1Dev d) {
+    if (SINGLE) {
+        if (d.g.n == 256) init_pass1_single<K, W, true>(d, blockIdx.x, gridDim.x);
+        else init_pass1_single<K, W, false>(d, blockIdx.x, gridDim.x);
+    } else {
+        init_pass1_body<K, W>(d, blockIdx.x, gridDim.x);
+    }
 }
 
 template <int K, int NWP, int G>
@@ -296,8 +302,11 @@ static void launch_init_pass1_s(const V1Dev& d, int grid, size_t sm, cudaStream_
 
 // Requires d.g.cover (cover_w 1, 2 or 4) and two columns.  Rows of one 256-robber block
 // split into whole lane pieces take the run form, which needs its tables in shared memory.
-void launch_init_pass1(const V1Dev& d, int grid, cudaStream_t st) {
+// One wave of resident blocks: each warp sweeps one contiguous range of configurations.
+void launch_init_pass1(const V1Dev& d, int num_sms, cudaStream_t st) {
     const bool single = d.g.n <= 256 && (d.g.n & 7) == 0;
+    const uint64_t cap = ((uint64_t)d.C + 7) / 8;
+    const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(cap, (uint64_t)num_sms * (single ? 3 : 4)));
     if (single) launch_init_pass1_s<true>(d, grid, (size_t)init_pass1_smem_words(d.g.n, d.g.rwp) * 4, st);
     else launch_init_pass1_s<false>(d, grid, 0, st);
 }

@@ -268,9 +268,8 @@ __device__ __forceinline__ void next_multiset(int (&c)[K], int n) {
 // keeps the masks of all cops but the last (they change once per n - c[k-2] steps).  Lane l
 // owns robbers 8l .. 8l+7 of each 256-vertex block, i.e. one 16-byte piece of the row, and
 // the 8-bit pieces of the marked and frontier rows, which four lanes assemble into a word.
-// The caller sets meta[0] = {0, 0, 0, 0, C, 0}, meta[1] = {1, empty, -1, 0, 0, 0}, every
-// column-0 flag to 1 and every column-1 flag to 0, and zeroes the pass counter; the pass
-// counter then holds the first pass's count.
+// The caller sets meta[0] = {0, 0, 0, 0, C, 0}, meta[1] = {1, empty, -1, 0, 0, 0} and zeroes
+// the pass counter; the pass counter then holds the first pass's count.
 // The same sweep for rows of one 256-robber block whose robbers split into whole lane pieces
 // (n <= 256, n a multiple of 8), organised around the common configuration.  Consecutive
 // configurations share their leading cops c[0 .. K-2] for a run of up to n of them (only the
@@ -287,21 +286,28 @@ __device__ __forceinline__ void next_multiset(int (&c)[K], int n) {
 // gains no mark and the configuration takes the fast form: the lane's 16-byte piece is a
 // shared-memory table entry indexed by its 8 column-0 seed bits, XORed with the leading cops'
 // patch and stored once; the last cop's two bytes follow as one 2-byte store; one store per
-// row word writes the marked words; nothing else is written (the column-1 frontier row and flag
-// stay as the caller cleared them).  Otherwise it takes the general form, which tests every
-// robber exactly, splits its column-1 marks by round, patches their bytes and writes the
-// frontier words.  Results are byte-identical to the general sweep.  Dynamic shared memory:
-// init_pass1_smem_words(n, rwp) words.
+// row word writes the marked words; nothing else is written (the column-1 frontier row stays
+// unwritten and its flag clear: the warp sets its configurations' flag bytes first).  The fast
+// form runs as a tight inner loop over per-lane cursors (piece, marked word, cover row,
+// neighbour word, the last cop's offsets) and leaves it only for a configuration that trips,
+// which takes the general form: every robber tested exactly, the column-1 marks split by round,
+// their bytes patched and the frontier words written.  FULL (n = 256) lets every lane own eight
+// robbers, which removes the lane predicates.  Results are byte-identical to the general sweep.
+// Dynamic shared memory: init_pass1_smem_words(n, rwp) words.
 __host__ __device__ inline int init_pass1_smem_words(int n, int rwp) { return 256 * 4 + n * rwp; }
 
-template <int K, int W>
+template <int K, int W, bool FULL>
 __device__ CR_BODY_INLINE void init_pass1_single(const V1Dev& d, unsigned wk, unsigned nwk) {
     extern __shared__ uint32_t sm[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int n = d.g.n, rw = d.g.rw, rwp = d.g.rwp, S = d.S, npad = d.g.npad;
-    const uint32_t* CR_RESTRICT nbr = d.g.nbr;
+    // FULL: n = 256 exactly, so every lane owns 8 robbers and every row word has a lane
+    const int n = FULL ? 256 : d.g.n, rw = FULL ? 8 : d.g.rw, rwp = FULL ? 8 : d.g.rwp;
+    const int S = d.S, npad = FULL ? 256 : d.g.npad;
+    const uint32_t C = d.C;
     const uint32_t* CR_RESTRICT iso = cop_iso(d.g);
     const uint8_t* CR_RESTRICT cover = d.g.cover;
+    uint8_t* const table = d.table;
+    uint32_t* const marked = d.marked;
     const size_t plane = (size_t)n * npad * W;
     const bool padded = rw != rwp || S > 2;
     // shared memory: the piece table (entry s: robbers j with bit j of s set read 0x03 in
@@ -315,27 +321,34 @@ __device__ CR_BODY_INLINE void init_pass1_single(const V1Dev& d, unsigned wk, un
         lut[t] = make_uint4(__byte_perm(s0, fe, 0x5140), __byte_perm(s0, fe, 0x7362),
                             __byte_perm(s1, fe, 0x5140), __byte_perm(s1, fe, 0x7362));
     }
-    for (int t = threadIdx.x; t < n * rwp; t += blockDim.x) snbr[t] = CR_LDG(&nbr[t]);
+    for (int t = threadIdx.x; t < n * rwp; t += blockDim.x) snbr[t] = CR_LDG(&d.g.nbr[t]);
     __syncthreads();
     unsigned cnt = 0, cnt1 = 0, rows1 = 0, any1 = 0, any2 = 0;
     const size_t nwarps = (size_t)nwk * (blockDim.x >> 5);
-    const size_t chunk = (d.C + nwarps - 1) / nwarps;
+    const size_t chunk = (C + nwarps - 1) / nwarps;
     const size_t cb = ((size_t)wk * (blockDim.x >> 5) + warp) * chunk;
-    const size_t ce = cb + chunk < d.C ? cb + chunk : d.C;
+    const size_t ce = cb + chunk < C ? cb + chunk : C;
     int c[K];
     if (cb < ce) {
 #pragma unroll
         for (int i = 0; i < K; ++i) c[i] = CR_LDG(&d.configs[cb * K + i]);
     }
     const int lr0 = lane * 8;                 // this lane's robbers lr0 .. lr0 + 7
-    const bool live = lr0 < n;
+    const bool live = FULL || lr0 < n;
     const int wi = lane >> 2;                 // their word of a robber row
     const int sh = (lane & 3) * 8;            // and their bit offset in it
     const uint32_t lvalid = live ? 0xFFu : 0u;
-    const bool writer = (lane & 3) == 0 && wi < rw;
+    const bool writer = (lane & 3) == 0 && (FULL || wi < rw);
     // fast form: lane 4w writes word w of the column-0 marked row, lane 4w + 1 that of column 1
-    const bool mwriter = (lane & 3) < 2 && wi < rw;
-    const size_t mplane = (lane & 1) ? (size_t)d.C * rwp : 0;
+    const bool mwriter = (lane & 3) < 2 && (FULL || wi < rw);
+    const size_t mplane = (lane & 1) ? (size_t)C * rwp : 0;
+    // the flag planes of this warp's configurations: column 0 set (every row holds captures),
+    // column 1 clear (set below for the rows that gain marks)
+    for (size_t i = cb + lane; i < ce; i += 32) {
+        d.fflag[i] = 1;
+        d.fflag[(size_t)C + i] = 0;
+    }
+    __syncwarp();
     size_t cid = cb;
     while (cid < ce) {
         // a new run of the leading cops c[0 .. K-2]: the AND of their uncovered masks (with and
@@ -366,48 +379,55 @@ __device__ CR_BODY_INLINE void init_pass1_single(const V1Dev& d, unsigned wk, un
         capx.y = ((cpre & 4u) ? 0x0000FFFFu : 0u) | ((cpre & 8u) ? 0xFFFF0000u : 0u);
         capx.z = ((cpre & 16u) ? 0x0000FFFFu : 0u) | ((cpre & 32u) ? 0xFFFF0000u : 0u);
         capx.w = ((cpre & 64u) ? 0x0000FFFFu : 0u) | ((cpre & 128u) ? 0xFFFF0000u : 0u);
-        int cl = c[K - 1];
-        const size_t run_end = cid + (size_t)(n - cl) < ce ? cid + (size_t)(n - cl) : ce;
-        uint8_t* dst = d.table + cid * n * 2 + lr0 * 2;
-        uint32_t* mrow = d.marked + mplane + cid * rwp + wi;
-        const uint8_t* cv = cover + (size_t)(cl * npad + lr0) * W;
-        for (; cid < run_end; ++cid, ++cl, dst += 2 * n, mrow += rwp, cv += (size_t)npad * W) {
-            const unsigned dl = (unsigned)(cl - lr0);
-            const uint32_t capb = cpre | (dl < 8u ? 1u << dl : 0u);
-            const uint32_t capw = cpw | ((cl >> 5) == wi ? 1u << (cl & 31) : 0u);
-            bool trip = false;
-            if (live) {
+        const int cl0 = c[K - 1];
+        const size_t cid0 = cid;
+        const uint32_t len = (uint32_t)(cid0 + (size_t)(n - cl0) < ce ? (size_t)(n - cl0) : ce - cid0);
+        cid += len;
+        // per-lane cursors of the run: the lane's piece, its marked word, its cover row (lanes
+        // without robbers read lane 0's), its neighbour word, the last cop's offset from the
+        // lane's robbers and from its row word
+        uint8_t* dst = table + cid0 * n * 2 + lr0 * 2;
+        uint32_t* mrow = marked + mplane + cid0 * rwp + wi;
+        const uint8_t* cv = cover + (size_t)(cl0 * npad + (live ? lr0 : 0)) * W;
+        const uint32_t* nb = snbr + cl0 * rwp + (live ? wi : 0);
+        int dl = cl0 - lr0, dw = cl0 - 32 * wi;
+        uint32_t j = 0;
+        while (j < len) {
+            // fast form while every cop can move and column 1 gains no mark
+            for (; j < len; ++j, dst += 2 * n, mrow += rwp, cv += npad * W, nb += rwp, ++dl, ++dw) {
                 Cov8<W> z;
                 z.load(cv);
                 z.andd(zpre);
-                trip = z.has_zero();
-            }
-            if (!__any_sync(FULL_MASK, trip) && mpre) {
-                // fast form: every cop can move and column 1 gains no mark
-                const uint32_t xw = live ? (npre | snbr[cl * rwp + wi]) : 0u;
-                const uint32_t seedb = (xw >> sh) & 0xFFu & ~capb;
-                if (live) {
-                    uint4 pc = lut[seedb];
-                    pc.x ^= capx.x;
-                    pc.y ^= capx.y;
-                    pc.z ^= capx.z;
-                    pc.w ^= capx.w;
-                    *reinterpret_cast<uint4*>(dst) = pc;
-                    if (dl < 8u) *reinterpret_cast<uint16_t*>(dst + 2 * dl) = 0x0101u;
-                }
+                if (__any_sync(FULL_MASK, live && z.has_zero()) || !mpre) break;
+                const uint32_t c2b = (unsigned)dl < 8u ? 1u << dl : 0u;
+                const uint32_t capw = cpw | ((unsigned)dw < 32u ? 1u << dw : 0u);
+                const uint32_t xw = npre | *nb;
+                const uint32_t seedb = (xw >> sh) & lvalid & ~(cpre | c2b);
+                uint4 pc = lut[seedb];
+                pc.x ^= capx.x;
+                pc.y ^= capx.y;
+                pc.z ^= capx.z;
+                pc.w ^= capx.w;
+                if (live) *reinterpret_cast<uint4*>(dst) = pc;
+                if (c2b) *reinterpret_cast<uint16_t*>(dst + 2 * dl) = 0x0101u;
                 cnt += __popc(seedb);
                 if (mwriter) *mrow = (lane & 1) ? capw : (xw | capw);
                 if (padded) {
-                    uint32_t* m0row = d.marked + cid * rwp;
-                    uint32_t* m1row = d.marked + ((size_t)d.C + cid) * rwp;
+                    uint32_t* m0row = marked + (cid0 + j) * rwp;
+                    uint32_t* m1row = marked + ((size_t)C + cid0 + j) * rwp;
                     for (int e = rw + lane; e < rwp; e += 32) {
                         m0row[e] = 0u;
                         m1row[e] = 0u;
                     }
                 }
-                continue;
             }
-            // general form
+            if (j >= len) break;
+            // general form of configuration cid0 + j
+            const int cl = cl0 + (int)j;
+            const size_t id = cid0 + j;
+            const unsigned dlu = (unsigned)dl;
+            const uint32_t capb = cpre | (dlu < 8u ? 1u << dlu : 0u);
+            const uint32_t capw = cpw | ((unsigned)dw < 32u ? 1u << dw : 0u);
             const bool moves = mpre && !((CR_LDG(&iso[cl >> 5]) >> (cl & 31)) & 1u);
             const uint32_t off = (uint32_t)(cl * npad + lr0) * W;
             uint32_t xw = 0, a = 0;
@@ -428,7 +448,7 @@ __device__ CR_BODY_INLINE void init_pass1_single(const V1Dev& d, unsigned wk, un
                 pc.z ^= capx.z;
                 pc.w ^= capx.w;
                 *reinterpret_cast<uint4*>(dst) = pc;
-                if (dl < 8u) *reinterpret_cast<uint16_t*>(dst + 2 * dl) = 0x0101u;
+                if (dlu < 8u) *reinterpret_cast<uint16_t*>(dst + 2 * dlu) = 0x0101u;
             }
             cnt += __popc(seedb);
             uint32_t m1w = capw;
@@ -445,12 +465,12 @@ __device__ CR_BODY_INLINE void init_pass1_single(const V1Dev& d, unsigned wk, un
                 const uint32_t a2 = a & deepb, a1 = a & ~deepb;
                 uint32_t sp = a;
                 while (sp) {
-                    const int j = __ffs(sp) - 1;
+                    const int jb = __ffs(sp) - 1;
                     sp &= sp - 1;
-                    const uint32_t bit = 1u << j;
+                    const uint32_t bit = 1u << jb;
                     const uint32_t v0 = (seedb & bit) ? 0x03u : 0xFEu;
                     const uint32_t v1 = (a1 & bit) ? 0x03u : 0x05u;
-                    *reinterpret_cast<uint16_t*>(dst + 2 * j) = (uint16_t)(v0 | (v1 << 8));
+                    *reinterpret_cast<uint16_t*>(dst + 2 * jb) = (uint16_t)(v0 | (v1 << 8));
                 }
                 cnt1 += __popc(a1) + __popc(a2);
                 any1 |= a1;
@@ -463,7 +483,7 @@ __device__ CR_BODY_INLINE void init_pass1_single(const V1Dev& d, unsigned wk, un
                 const uint32_t t01 = __byte_perm(v, v1, 0x5140), t23 = __byte_perm(v2, v3, 0x5140);
                 const uint32_t a1w = __byte_perm(t01, t23, 0x5410), a2w = __byte_perm(t01, t23, 0x7632);
                 m1w |= a1w | a2w;
-                uint32_t* frow = d.front + ((size_t)d.C + cid) * (size_t)(S * rwp);
+                uint32_t* frow = d.front + ((size_t)C + id) * (size_t)(S * rwp);
                 if (writer) {
                     frow[wi] = a1w;
                     frow[rwp + wi] = a2w;
@@ -475,13 +495,13 @@ __device__ CR_BODY_INLINE void init_pass1_single(const V1Dev& d, unsigned wk, un
                     }
                     for (int e = 2 * rwp + lane; e < S * rwp; e += 32) frow[e] = 0u;
                 }
-                if (lane == 0) {   // the caller set every column-0 flag and cleared column 1's
-                    d.fflag[(size_t)d.C + cid] = 1;
+                if (lane == 0) {
+                    d.fflag[(size_t)C + id] = 1;
                     ++rows1;
                 }
             }
-            uint32_t* m0row = d.marked + cid * rwp;
-            uint32_t* m1row = d.marked + ((size_t)d.C + cid) * rwp;
+            uint32_t* m0row = marked + id * rwp;
+            uint32_t* m1row = marked + ((size_t)C + id) * rwp;
             if (writer) {
                 m0row[wi] = xw | capw;
                 m1row[wi] = m1w;
@@ -492,6 +512,13 @@ __device__ CR_BODY_INLINE void init_pass1_single(const V1Dev& d, unsigned wk, un
                     m1row[e] = 0u;
                 }
             }
+            ++j;
+            dst += 2 * n;
+            mrow += rwp;
+            cv += npad * W;
+            nb += rwp;
+            ++dl;
+            ++dw;
         }
         // the run is over: step the multiset past its last configuration
         if (cid < ce) {

@@ -78,7 +78,10 @@ struct cr_solver {
     uint8_t* d_fflag = nullptr;
     uint32_t* d_cand = nullptr;
     uint32_t* d_h1 = nullptr;   // k = 3: H1 rows of the separable dense cop turn
-    uint8_t* d_cflag = nullptr;
+    uint32_t* d_cbits = nullptr;      // push-mode candidate bitmap
+    uint32_t* d_list = nullptr;       // [cols][C] row lists of the frontiers
+    uint32_t* d_clist = nullptr;      // [C] push-mode candidate list
+    unsigned* d_sync = nullptr;       // [2] prep's block count, candidate count
     uint32_t* d_rrp = nullptr;
     uint16_t* d_rcol = nullptr;
     uint32_t* d_nbr = nullptr;
@@ -254,7 +257,8 @@ uint64_t cr_solver_footprint(int32_t n, int32_t k, int32_t p, int32_t rules) {
     uint64_t b = C * (uint64_t)n * cols;                 // table
     b += (uint64_t)cols * C * rwp * 4;                   // marked
     b += (uint64_t)cols * C * S * rwp * 4;               // frontiers
-    b += C * S * rwp * 4 + C;                            // push-mode candidate rows and flags
+    b += C * S * rwp * 4 + cand_bits_bytes(C) + C * 4;   // push-mode candidate rows, bitmap, list
+    b += (uint64_t)cols * C * 4 + 2 * sizeof(unsigned);  // frontier row lists, prep/list counters
     b += h1_bytes(n, k, S, rwp);                         // separable dense cop turn (k = 3)
     b += (uint64_t)cols * C;                             // flags
     b += C * (uint64_t)k * 2;                            // configs
@@ -275,14 +279,16 @@ static void free_v1(cr_solver* s) {
     s->d_hist_n = nullptr;
     void* ptrs[] = {s->d_rp, s->d_col, s->d_binom, s->d_configs, s->d_hop, s->d_table,
                     s->d_marked, s->d_front, s->d_fflag, s->d_meta, s->d_counters, s->d_err,
-                    s->d_heads, s->d_trans, s->d_cand, s->d_cflag, s->d_rrp, s->d_rcol, s->d_nbr, s->d_iso, s->d_rhop, s->d_cover,
+                    s->d_heads, s->d_trans, s->d_cand, s->d_cbits, s->d_list, s->d_clist, s->d_sync,
+                    s->d_rrp, s->d_rcol, s->d_nbr, s->d_iso, s->d_rhop, s->d_cover,
                     s->d_crp, s->d_ccol, s->d_ciso, s->d_h1};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     s->d_rp = nullptr; s->d_col = nullptr; s->d_binom = nullptr; s->d_configs = nullptr;
     s->d_hop = nullptr; s->d_table = nullptr; s->d_marked = nullptr; s->d_front = nullptr;
     s->d_fflag = nullptr; s->d_meta = nullptr; s->d_counters = nullptr; s->d_err = nullptr;
-    s->d_heads = nullptr; s->d_trans = nullptr; s->d_cand = nullptr; s->d_cflag = nullptr;
+    s->d_heads = nullptr; s->d_trans = nullptr; s->d_cand = nullptr; s->d_cbits = nullptr;
+    s->d_list = nullptr; s->d_clist = nullptr; s->d_sync = nullptr;
     s->d_rrp = nullptr; s->d_rcol = nullptr; s->d_nbr = nullptr; s->d_iso = nullptr; s->d_rhop = nullptr;
     s->d_cover = nullptr;
     s->d_crp = nullptr; s->d_ccol = nullptr; s->d_ciso = nullptr; s->d_h1 = nullptr;
@@ -327,7 +333,10 @@ static V1Dev dev_view(const cr_solver* s) {
     d.fflag = s->d_fflag;
     d.cand = s->d_cand;
     d.h1 = s->d_h1;
-    d.cflag = s->d_cflag;
+    d.cbits = s->d_cbits;
+    d.list = s->d_list;
+    d.clist = s->d_clist;
+    d.sync = s->d_sync;
     d.meta = s->d_meta;
     d.pass_new = s->d_counters;
     d.err = s->d_err;
@@ -363,9 +372,12 @@ static int alloc_v1(cr_solver* s) {
     CR_CUDA(ctx, cudaMalloc(&s->d_fflag, (size_t)s->cols * C));
     CR_CUDA(ctx, cudaMalloc(&s->d_meta, sizeof(ColMeta) * s->cols));
     CR_CUDA(ctx, cudaMalloc(&s->d_cand, C * s->S * s->rwp * 4));
-    CR_CUDA(ctx, cudaMalloc(&s->d_cflag, C));
+    CR_CUDA(ctx, cudaMalloc(&s->d_cbits, cand_bits_bytes(C)));
+    CR_CUDA(ctx, cudaMalloc(&s->d_list, (size_t)s->cols * C * 4));
+    CR_CUDA(ctx, cudaMalloc(&s->d_clist, C * 4));
+    CR_CUDA(ctx, cudaMalloc(&s->d_sync, 2 * sizeof(unsigned)));
     CR_CUDA(ctx, cudaMemsetAsync(s->d_cand, 0, C * s->S * s->rwp * 4, ctx->stream));
-    CR_CUDA(ctx, cudaMemsetAsync(s->d_cflag, 0, C, ctx->stream));
+    CR_CUDA(ctx, cudaMemsetAsync(s->d_cbits, 0, cand_bits_bytes(C), ctx->stream));
     if (const uint64_t hb = h1_bytes(s->n, s->k, s->S, s->rwp)) CR_CUDA(ctx, cudaMalloc(&s->d_h1, hb));
     CR_CUDA(ctx, cudaMalloc(&s->d_hop, (size_t)s->n * s->rwp * 4));
     std::vector<uint32_t> hop = hop_masks(s);
@@ -614,10 +626,12 @@ static int v1_init(cr_solver* s, uint64_t* caps) {
     CR_CUDA(ctx, cudaMemsetAsync(s->d_counters, 0, 4 * sizeof(unsigned long long), st));
     CR_CUDA(ctx, cudaMemsetAsync(s->d_err, 0, sizeof(unsigned), st));
     std::vector<ColMeta> meta(s->cols);
-    for (int c = 0; c < s->cols; ++c) meta[c] = ColMeta{0, kEmptyLo, -1, 0, 0, 0, {0, 0}};
-    // capture seeds in columns 0 and 1; pass 1's column-0 producer appends to column 0's
-    meta[0] = ColMeta{0, 0, 0, 1, (int)std::min<uint64_t>(C, INT32_MAX), 0, {0, 0}};
-    meta[1] = ColMeta{0, 0, 0, 0, (int)std::min<uint64_t>(C, INT32_MAX), 1, {0, 0}};
+    for (int c = 0; c < s->cols; ++c) meta[c] = ColMeta{0, kEmptyLo, -1, 0, 0, 0, 0, 0};
+    // capture seeds in columns 0 and 1 (every row: the implicit list); pass 1's column-0
+    // producer appends to column 0's
+    meta[0] = ColMeta{0, 0, 0, 1, (int)std::min<uint64_t>(C, INT32_MAX), 0, -1, 0};
+    meta[1] = ColMeta{0, 0, 0, 0, (int)std::min<uint64_t>(C, INT32_MAX), 1, -1, 0};
+    CR_CUDA(ctx, cudaMemsetAsync(s->d_sync, 0, 2 * sizeof(unsigned), st));
     CR_CUDA(ctx, cudaMemcpyAsync(s->d_meta, meta.data(), sizeof(ColMeta) * s->cols, cudaMemcpyHostToDevice, st));
     V1Dev d = dev_view(s);
     launch_init(d, s->grid_small, st);
@@ -641,8 +655,11 @@ static int v1_init_pass1(cr_solver* s, uint64_t* found) {
     cudaStream_t st = ctx->stream;
     CR_CUDA(ctx, cudaMemsetAsync(s->d_counters, 0, 4 * sizeof(unsigned long long), st));
     CR_CUDA(ctx, cudaMemsetAsync(s->d_err, 0, sizeof(unsigned), st));
-    ColMeta meta[2] = {ColMeta{0, 0, 0, 0, (int)std::min<uint64_t>(s->C, INT32_MAX), 0, {0, 0}},
-                       ColMeta{1, kEmptyLo, -1, 0, 0, 0, {0, 0}}};
+    // column 0's frontier after pass 1 is every row (the implicit list), column 1's the rows
+    // the kernel lists
+    ColMeta meta[2] = {ColMeta{0, 0, 0, 0, (int)std::min<uint64_t>(s->C, INT32_MAX), 0, -1, 0},
+                       ColMeta{1, kEmptyLo, -1, 0, 0, 0, 0, 0}};
+    CR_CUDA(ctx, cudaMemsetAsync(s->d_sync, 0, 2 * sizeof(unsigned), st));
     CR_CUDA(ctx, cudaMemcpyAsync(s->d_meta, meta, sizeof(meta), cudaMemcpyHostToDevice, st));
     V1Dev d = dev_view(s);
     CR_CUDA(ctx, cudaEventRecord(s->evc0, st));
@@ -783,7 +800,7 @@ static int grow_slots_and_replay(cr_solver* s) {
     CR_CUDA(ctx, cudaMalloc(&s->d_front, (size_t)s->cols * s->C * s->S * s->rwp * 4));
     CR_CUDA(ctx, cudaMalloc(&s->d_cand, (size_t)s->C * s->S * s->rwp * 4));
     CR_CUDA(ctx, cudaMemsetAsync(s->d_cand, 0, (size_t)s->C * s->S * s->rwp * 4, ctx->stream));
-    CR_CUDA(ctx, cudaMemsetAsync(s->d_cflag, 0, s->C, ctx->stream));
+    CR_CUDA(ctx, cudaMemsetAsync(s->d_cbits, 0, cand_bits_bytes(s->C), ctx->stream));
     if (const uint64_t hb = h1_bytes(s->n, s->k, s->S, s->rwp)) CR_CUDA(ctx, cudaMalloc(&s->d_h1, hb));
     const int per_sm = max_cop_blocks_per_sm(s->k, s->rwp, s->S);
     s->grid_cop = (int)std::max<uint64_t>(1, std::min<uint64_t>((s->C + 7) / 8, (uint64_t)ctx->num_sms * per_sm));

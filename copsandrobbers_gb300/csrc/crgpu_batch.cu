@@ -83,8 +83,8 @@ __host__ __device__ inline uint64_t binom_dev(int64_t n, int64_t k) {
 
 // Byte offsets of one (n, k, p) solve inside a slot.
 struct JobLayout {
-    size_t binom, configs, nbr, iso, hop, rhop, table, marked, front, h1, fflag, cand, cflag, meta,
-        counters, err, total;
+    size_t binom, configs, nbr, iso, hop, rhop, table, marked, front, h1, list, clist, fflag, cand,
+        cbits, sync, meta, counters, err, total;
 };
 
 __host__ __device__ inline JobLayout job_layout(int n, int k, int p, int S) {
@@ -109,9 +109,13 @@ __host__ __device__ inline JobLayout job_layout(int n, int k, int p, int S) {
     // k = 3: rows of the separable dense cop turn (written before they are read each pass,
     // so they sit outside the regions the block zeroes)
     L.h1 = take(k == 3 ? (size_t)n * (n + 1) / 2 * n * S * rwp * 4 : 0);
+    // frontier row lists and the push-mode candidate list (written before they are read)
+    L.list = take((size_t)cols * C * 4);
+    L.clist = take(C * 4);
     L.fflag = take((size_t)cols * C);
     L.cand = take(C * S * rwp * 4);
-    L.cflag = take(C);
+    L.cbits = take(cand_bits_bytes(C));
+    L.sync = take(2 * sizeof(unsigned));
     L.meta = take(sizeof(ColMeta) * cols);
     L.counters = take(4 * sizeof(unsigned long long));
     L.err = take(sizeof(unsigned));
@@ -178,7 +182,10 @@ __device__ int solve_job(const BatchDev& b, unsigned char* slot, int gi, int jr,
     d.fflag = slot + L.fflag;
     d.cand = reinterpret_cast<uint32_t*>(slot + L.cand);
     d.h1 = K == 3 ? reinterpret_cast<uint32_t*>(slot + L.h1) : nullptr;
-    d.cflag = slot + L.cflag;
+    d.cbits = reinterpret_cast<uint32_t*>(slot + L.cbits);
+    d.list = reinterpret_cast<uint32_t*>(slot + L.list);
+    d.clist = reinterpret_cast<uint32_t*>(slot + L.clist);
+    d.sync = reinterpret_cast<unsigned*>(slot + L.sync);
     d.meta = reinterpret_cast<ColMeta*>(slot + L.meta);
     d.pass_new = reinterpret_cast<unsigned long long*>(slot + L.counters);
     d.err = reinterpret_cast<unsigned*>(slot + L.err);
@@ -257,9 +264,9 @@ __device__ int solve_job(const BatchDev& b, unsigned char* slot, int gi, int jr,
     }
     // ---- initializeCaptures
     if (threadIdx.x == 0) {
-        for (int c = 0; c < cols; ++c) d.meta[c] = ColMeta{0, kEmptyLo, -1, 0, 0, 0, {0, 0}};
-        d.meta[0] = ColMeta{0, 0, 0, 1, (int)C, 0, {0, 0}};
-        d.meta[1] = ColMeta{0, 0, 0, 0, (int)C, 1, {0, 0}};
+        for (int c = 0; c < cols; ++c) d.meta[c] = ColMeta{0, kEmptyLo, -1, 0, 0, 0, 0, 0};
+        d.meta[0] = ColMeta{0, 0, 0, 1, (int)C, 0, -1, 0};
+        d.meta[1] = ColMeta{0, 0, 0, 0, (int)C, 1, -1, 0};
     }
     __syncthreads();
     init_body(d, K, 0, 1);

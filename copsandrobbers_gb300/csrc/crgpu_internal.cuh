@@ -8,6 +8,7 @@
 //   front   uint32 [cols][C][S][rwp] marks the column's last producer run made, split by
 //                                    value: slot s holds the states of value base + s
 //   fflag   uint8  [cols][C]         1 = row C of the column's frontier is non-empty
+//   list    uint32 [cols][C]         the ids of those rows, in append order (meta.len of them)
 //   configs uint16 [C][k]            sorted cop multisets in lexicographic order (AuxGraph.h:117-177)
 // rw = ceil(n / 32) words of robber bits per row; rwp pads rw to 1, 2 or a multiple of 4 so
 // that a row starts on a 16-byte boundary and loads as uint4 vectors.
@@ -38,8 +39,13 @@ struct ColMeta {
     int append;  // 1 = the next producer run adds to the frontier instead of replacing it
     int rows;    // configurations whose frontier row is non-empty
     int seed;    // 1 = the frontier is exactly the capture seeds (r on a cop, value 0)
-    int pad[2];
+    int len;     // rows in the column's list; -1 = every configuration (the list is implicit)
+    int clean;   // 1 = the frontier's consumer has cleared the flags of the listed rows
 };
+
+// Candidate rows of the push-mode cop turn: a bitmap of C bits marks the configurations that
+// received a candidate row; its bytes (rounded up to whole words).
+__host__ __device__ inline size_t cand_bits_bytes(uint64_t C) { return (size_t)((C + 31) / 32) * 4; }
 
 struct DevGraph {
     int n;
@@ -94,7 +100,10 @@ struct V1Dev {
     // k = 3 dense cop turns: H1 rows [P][n][S][rwp], P = n(n+1)/2 pairs {x <= y}; H1[{x,y}][c]
     // = OR over z in N(c) of the frontier row of sort(x, y, z).  Null = the tuple-gathering pull.
     uint32_t* h1 = nullptr;
-    uint8_t* cflag;           // [C]: 1 = cand row non-empty
+    uint32_t* cbits;          // [ceil(C / 32)]: bit C set = cand row C non-empty
+    uint32_t* list;           // [cols][C]: the row lists of the columns' frontiers
+    uint32_t* clist;          // [C]: ids of the non-empty cand rows (sync[1] of them)
+    unsigned* sync;           // [2]: blocks done with the current prep, cand rows listed
     ColMeta* meta;            // [cols]
     unsigned long long* pass_new;
     unsigned int* err;

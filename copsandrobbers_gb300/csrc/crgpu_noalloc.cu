@@ -78,7 +78,7 @@ int scratch_base(int device, unsigned char** out, char* err, size_t err_len) {
 // Byte offsets of every buffer inside the scratch area (256-byte aligned).
 struct Layout {
     size_t rp, col, rrp, rcol, cursor, nbr, iso, hop, rhop, binom, configs, marked, front, fflag,
-        cand, cflag, meta, counters, err, total;
+        cand, cbits, list, clist, sync, meta, counters, err, total;
 };
 
 Layout plan(int n, size_t nnz, int k, int cols, uint64_t C, int rwp, int S) {
@@ -105,7 +105,10 @@ Layout plan(int n, size_t nnz, int k, int cols, uint64_t C, int rwp, int S) {
     L.front = take((size_t)cols * C * S * rwp * 4);
     L.fflag = take((size_t)cols * C);
     L.cand = take(C * S * rwp * 4);
-    L.cflag = take(C);
+    L.cbits = take(cand_bits_bytes(C));
+    L.list = take((size_t)cols * C * 4);
+    L.clist = take(C * 4);
+    L.sync = take(2 * sizeof(unsigned));
     L.meta = take(sizeof(ColMeta) * cols);
     L.counters = take(4 * sizeof(unsigned long long));
     L.err = take(sizeof(unsigned));
@@ -276,6 +279,7 @@ extern "C" int cr_solve_v1_noalloc(const cr_graph* g, int32_t k, int32_t p, void
         d.g.nbr = reinterpret_cast<const uint32_t*>(base + L.nbr);
         d.g.isolated = reinterpret_cast<const uint32_t*>(base + L.iso);
         d.g.rhop = reinterpret_cast<const uint32_t*>(base + L.rhop);
+        d.g.nnz = (int)nnz;   // lets the last column stage the graph in shared memory
         int maxdeg = 0;
         for (int v = 0; v < n; ++v) maxdeg = maxdeg > (int)(g->row_ptr[v + 1] - g->row_ptr[v]) ? maxdeg : (int)(g->row_ptr[v + 1] - g->row_ptr[v]);
         d.g.maxdeg = maxdeg;
@@ -291,7 +295,10 @@ extern "C" int cr_solve_v1_noalloc(const cr_graph* g, int32_t k, int32_t p, void
         d.front = reinterpret_cast<uint32_t*>(base + L.front);
         d.fflag = base + L.fflag;
         d.cand = reinterpret_cast<uint32_t*>(base + L.cand);
-        d.cflag = base + L.cflag;
+        d.cbits = reinterpret_cast<uint32_t*>(base + L.cbits);
+        d.list = reinterpret_cast<uint32_t*>(base + L.list);
+        d.clist = reinterpret_cast<uint32_t*>(base + L.clist);
+        d.sync = reinterpret_cast<unsigned*>(base + L.sync);
         d.meta = reinterpret_cast<ColMeta*>(base + L.meta);
         d.pass_new = reinterpret_cast<unsigned long long*>(base + L.counters);
         d.err = reinterpret_cast<unsigned*>(base + L.err);
@@ -313,10 +320,10 @@ extern "C" int cr_solve_v1_noalloc(const cr_graph* g, int32_t k, int32_t p, void
 
         // initializeCaptures (k_cops_visibility.cpp:85-127)
         ColMeta meta[126];
-        for (int c = 0; c < cols; ++c) meta[c] = ColMeta{0, kEmptyLo, -1, 0, 0, 0, {0, 0}};
+        for (int c = 0; c < cols; ++c) meta[c] = ColMeta{0, kEmptyLo, -1, 0, 0, 0, 0, 0};
         const int rows = C < 0x7FFFFFFFull ? (int)C : 0x7FFFFFFF;
-        meta[0] = ColMeta{0, 0, 0, 1, rows, 0, {0, 0}};
-        meta[1] = ColMeta{0, 0, 0, 0, rows, 1, {0, 0}};
+        meta[0] = ColMeta{0, 0, 0, 1, rows, 0, -1, 0};
+        meta[1] = ColMeta{0, 0, 0, 0, rows, 1, -1, 0};
         NA_CUDA(cudaMemcpyAsync(d.meta, meta, sizeof(ColMeta) * cols, cudaMemcpyHostToDevice, st));
         NA_CUDA(cudaMemsetAsync(states_dev, kUnmarked, table_bytes, st));
         launch_init(d, gsmall > 0 ? gsmall : 1, st);

@@ -75,31 +75,69 @@ struct Tally {
     }
 };
 
-// Before a producer run of column `col` (whose inputs are column nx): fix the value base of
-// its output frontier, reset the range, and clear the frontier flags -- unless the column is
-// in append mode (column 0 in pass 1, whose frontier already holds the capture seeds).
+// Before a producer run of column `col` (whose inputs are column nx): clear the flags of the
+// column's previous frontier unless its consumer already did (consumers that walk the row list
+// clear each row's flag as they take it; the dense cop turns read flags at random and leave
+// them), then fix the value base of the new frontier and empty its range and list -- unless
+// the column is in append mode (column 0 in pass 1 after the unfused initializeCaptures, whose
+// frontier already holds the capture seeds).  Every block reads the column's state first; the
+// last block to finish (counted in sync[0]) resets it, so no block reads a half-reset state.
 __device__ CR_BODY_INLINE void prep_body(const V1Dev& d, int col, int nx, unsigned wk, unsigned nwk) {
     ColMeta* mo = d.meta + col;
-    const int append = mo->append;
-    if (wk == 0 && threadIdx.x == 0) {
-        if (!append) {
-            const ColMeta mi = d.meta[nx];
-            mo->base = (mi.hi >= mi.lo) ? mi.lo + 1 : 0;
-            mo->lo = kEmptyLo;
-            mo->hi = -1;
-            mo->rows = 0;
-        }
-        mo->seed = 0;
-        if (col == 0) *d.pass_new = 0ull;
-        if (col == d.cols - 1) d.meta[0].append = 0;  // column 0's seeded frontier is consumed
-    }
-    if (!append) {
+    const int append = mo->append, clean = mo->clean;
+    if (!append && !clean) {
         uint8_t* f = d.fflag + (size_t)col * d.C;
-        for (size_t i = (size_t)wk * blockDim.x + threadIdx.x; i < d.C;
-             i += (size_t)nwk * blockDim.x)
+        for (size_t i = (size_t)wk * blockDim.x + threadIdx.x; i < d.C; i += (size_t)nwk * blockDim.x)
             f[i] = 0;
     }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        bool last = nwk == 1;
+        if (!last) {
+            __threadfence();
+            last = atomicAdd(&d.sync[0], 1u) == nwk - 1;
+        }
+        if (last) {
+            __threadfence();
+            if (nwk > 1) d.sync[0] = 0u;
+            if (!append) {
+                const ColMeta mi = d.meta[nx];
+                mo->base = (mi.hi >= mi.lo) ? mi.lo + 1 : 0;
+                mo->lo = kEmptyLo;
+                mo->hi = -1;
+                mo->rows = 0;
+                mo->len = 0;
+                mo->clean = 0;
+            }
+            mo->seed = 0;
+            if (col == 0) *d.pass_new = 0ull;
+            if (col % 2 == 0) d.sync[1] = 0u;                // the push form's candidate list
+            if (col == d.cols - 1) d.meta[0].append = 0;   // column 0's seeded frontier is consumed
+        }
+    }
 }
+
+// Appends `id` to column col's row list for every lane whose pred is set (warp-collective:
+// every lane of the warp calls it; one atomic per warp).
+__device__ __forceinline__ void list_append(const V1Dev& d, int col, bool pred, uint32_t id) {
+    const unsigned b = __ballot_sync(FULL_MASK, pred);
+    if (!b) return;
+    const int lane = threadIdx.x & 31, leader = __ffs(b) - 1;
+    int at = 0;
+    if (lane == leader) at = atomicAdd(&d.meta[col].len, __popc(b));
+    at = __shfl_sync(FULL_MASK, at, leader);
+    if (pred) d.list[(size_t)col * d.C + at + __popc(b & ((1u << lane) - 1u))] = id;
+}
+
+// The row list of a column's frontier as a consumer sees it: n entries, entry i = row id(i).
+struct RowList {
+    const uint32_t* ids;
+    uint32_t n;
+    bool all;
+    __device__ RowList(const V1Dev& d, int col, const ColMeta& m)
+        : ids(d.list + (size_t)col * d.C), n(m.len < 0 ? d.C : (uint32_t)m.len), all(m.len < 0) {}
+    __device__ __forceinline__ uint32_t id(uint32_t i) const { return all ? i : CR_LDG(&ids[i]); }
+};
 
 // initializeCaptures (k_cops_visibility.cpp:85-127): the table was memset to 0xFE; a robber
 // on a cop is a capture of round 0 in columns 0 and 1 only.  The seeds also form the first
@@ -499,6 +537,7 @@ __device__ CR_BODY_INLINE void init_pass1_single(const V1Dev& d, unsigned wk, un
                     d.fflag[(size_t)C + id] = 1;
                     ++rows1;
                 }
+                list_append(d, 1, lane == 0, (uint32_t)id);
             }
             uint32_t* m0row = marked + id * rwp;
             uint32_t* m1row = marked + ((size_t)C + id) * rwp;
@@ -731,6 +770,7 @@ __device__ CR_BODY_INLINE void init_pass1_body(const V1Dev& d, unsigned wk, unsi
             *fl1 = changed ? 1 : 0;
             rows1 += changed ? 1u : 0u;
         }
+        list_append(d, 1, lane == 0 && changed, (uint32_t)cid);
     }
     cnt = __reduce_add_sync(FULL_MASK, cnt);
     rows1 = __reduce_add_sync(FULL_MASK, rows1);
@@ -798,7 +838,8 @@ __device__ __forceinline__ void emit_row(const V1Dev& d, uint32_t cid, bool vali
         }
     }
     __syncwarp();
-    if (L.any(any != 0)) {
+    const bool newrow = L.any(any != 0);
+    if (newrow) {
         if (gl < rw) {
             d.marked[((size_t)col * d.C + cid) * rwp + gl] = mm;
             t.cnt += __popc(mm ^ m);
@@ -831,6 +872,8 @@ __device__ __forceinline__ void emit_row(const V1Dev& d, uint32_t cid, bool vali
             }
         }
     }
+    // (in append mode every row is already listed: the list is the implicit one)
+    list_append(d, col, newrow && gl == 0 && !append, cid);
     __syncwarp();
 }
 
@@ -1257,135 +1300,98 @@ __device__ CR_BODY_INLINE void cop_seed_body(const V1Dev& d, int col, int nx, un
     t.flush(d, col, L.lane);
 }
 
-// Visits the set flags of f[0 .. C) warp by warp (the sparse producers: push, apply, direct,
-// last column).  Groups of 32 configurations go to the warps round robin (group g to warp
-// g mod W, so that flags clustered in configuration order still spread over all warps); a warp
-// loads the flags of its next kFlagTile groups at once, so they cost one memory round trip
-// instead of one each.  next() hands out, warp-uniformly, each group with a set flag: act has
-// bit l set iff configuration base + l is flagged.
-constexpr int kFlagTile = 16;
-struct FlagScan {
-    const uint8_t* f;
-    size_t C, g0, nwarps;
-    int lane;
-    unsigned mine = 0, groups = 0;
-    bool first = true;
-    __device__ __forceinline__ FlagScan(const uint8_t* f_, size_t C_, unsigned wk, unsigned nwk) : f(f_), C(C_) {
-        lane = threadIdx.x & 31;
-        nwarps = (size_t)nwk * (blockDim.x >> 5);
-        g0 = (size_t)wk * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    }
-    __device__ __forceinline__ bool next(size_t& base, unsigned& act) {
-        while (!groups) {
-            if (!first) g0 += kFlagTile * nwarps;
-            first = false;
-            if (g0 * 32 >= C) return false;
-            uint8_t v[kFlagTile];
-#pragma unroll
-            for (int j = 0; j < kFlagTile; ++j) {
-                const size_t i = (g0 + j * nwarps) * 32 + lane;
-                v[j] = i < C ? f[i] : (uint8_t)0;
-            }
-            mine = 0;   // lane j < kFlagTile holds the ballot of group g0 + j * nwarps
-#pragma unroll
-            for (int j = 0; j < kFlagTile; ++j) {
-                const unsigned b = __ballot_sync(FULL_MASK, v[j] != 0);
-                if (lane == j) mine = b;
-            }
-            groups = __ballot_sync(FULL_MASK, mine != 0u);
-        }
-        const int j = __ffs(groups) - 1;
-        groups &= groups - 1;
-        base = (g0 + j * nwarps) * 32;
-        act = __shfl_sync(FULL_MASK, mine, j);
-        return true;
-    }
-};
-
-// Sparse cop turn, scatter: every non-empty frontier row of column nx is ORed into the
-// candidate rows of its predecessors (the product of the cops' in-neighbour lists).
+// Sparse cop turn, scatter: every row of column nx's frontier list is ORed into the candidate
+// rows of its predecessors (the product of the cops' in-neighbour lists).  A warp takes one list
+// entry at a time (entries go to the warps round robin, so the work per warp is one entry's
+// predecessor count, whatever the rows' order) and its lanes take the predecessor tuples.  The
+// first scatter into a candidate row lists it: a test-and-set in the candidate bitmap, and one
+// list atomic per warp and round.  Each entry's flag is cleared as it is taken.
 template <int K>
 __device__ CR_BODY_INLINE void cop_push_body(const V1Dev& d, int col, int nx, unsigned wk, unsigned nwk) {
     extern __shared__ uint32_t sm[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int n = d.g.n, rwp = d.g.rwp, S = d.S;
     const ColMeta mi = d.meta[nx];
-    if (mi.hi < mi.lo || mi.seed || !frontier_sparse(mi, d.C)) return;
+    if (mi.seed || !frontier_sparse(mi, d.C)) return;           // a dense form takes this frontier
+    if (wk == 0 && threadIdx.x == 0) d.meta[nx].clean = 1;   // every listed flag is cleared below
+    if (mi.hi < mi.lo) return;
     const int s_used = min(mi.hi - mi.base + 1, S);
     const int nwords = s_used * rwp;
     uint32_t* wrow = sm + warp * (S * rwp);
     const uint32_t* CR_RESTRICT fin = d.front + (size_t)nx * d.C * S * rwp;
-    const uint8_t* CR_RESTRICT fflag_in = d.fflag + (size_t)nx * d.C;
+    uint8_t* fflag_in = d.fflag + (size_t)nx * d.C;
     const uint32_t* CR_RESTRICT rrp = d.g.rrow_ptr;
     const uint16_t* CR_RESTRICT radj = d.g.rcol;
     const int np1 = n + 1;
+    const RowList rl(d, nx, mi);
     unsigned err = 0;
-    FlagScan scan(fflag_in, d.C, wk, nwk);
-    size_t base;
-    unsigned act;
-    while (scan.next(base, act)) {
-        while (act) {
-            const uint32_t cp = (uint32_t)(base + __ffs(act) - 1);
-            act &= act - 1;
-            const uint32_t* row = fin + (size_t)cp * S * rwp;
-            uint32_t nz = 0;
-            for (int e = lane; e < nwords; e += 32) {
-                wrow[e] = row[e];
-                if (wrow[e]) nz = 1;
-            }
-            const bool any = __any_sync(FULL_MASK, nz != 0);
-            __syncwarp();
-            if (any) {
-                const uint16_t* cc = d.configs + (size_t)cp * K;
-                int lo[K], dg[K];
-                int T = 1;
+    const uint32_t nwarps = nwk * (blockDim.x >> 5);
+    for (uint32_t i = wk * (blockDim.x >> 5) + warp; i < rl.n; i += nwarps) {
+        const uint32_t cp = rl.id(i);
+        const uint32_t* row = fin + (size_t)cp * S * rwp;
+        uint32_t nz = 0;
+        for (int e = lane; e < nwords; e += 32) {
+            const uint32_t v = row[e];
+            wrow[e] = v;
+            nz |= v;
+        }
+        if (lane == 0) fflag_in[cp] = 0;
+        const bool any = __any_sync(FULL_MASK, nz != 0);
+        __syncwarp();
+        if (any) {
+            const uint16_t* cc = d.configs + (size_t)cp * K;
+            int lo[K], dg[K];
+            int T = 1;
 #pragma unroll
-                for (int i = 0; i < K; ++i) {
-                    const int v = cc[i];
-                    lo[i] = CR_LDG(&rrp[v]);
-                    dg[i] = CR_LDG(&rrp[v + 1]) - lo[i];
-                    T *= dg[i];
-                }
-                for (int tt = lane; tt < T; tt += 32) {
+            for (int q = 0; q < K; ++q) {
+                const int v = cc[q];
+                lo[q] = CR_LDG(&rrp[v]);
+                dg[q] = CR_LDG(&rrp[v + 1]) - lo[q];
+                T *= dg[q];
+            }
+            for (int t0 = 0; t0 < T; t0 += 32) {   // T is the warp's: every lane runs each round
+                const int tt = t0 + lane;
+                bool fresh = false;
+                uint32_t pc = 0;
+                if (tt < T) {
                     int c[K];
                     int rem = tt;
 #pragma unroll
-                    for (int i = K - 1; i >= 0; --i) {
-                        const int q = rem / dg[i];
-                        c[i] = CR_LDG(&radj[lo[i] + rem - q * dg[i]]);
-                        rem = q;
+                    for (int q = K - 1; q >= 0; --q) {
+                        const int qq = rem / dg[q];
+                        c[q] = CR_LDG(&radj[lo[q] + rem - qq * dg[q]]);
+                        rem = qq;
                     }
                     sort_small<K>(c);
-                    const uint32_t pc = rank_g<K>(c, d.binom, np1);
-                    if (pc >= d.C) { err |= kErrRank; continue; }
-                    uint32_t* crow = d.cand + (size_t)pc * S * rwp;
-                    for (int e = 0; e < nwords; ++e)
-                        if (wrow[e]) atomicOr(&crow[e], wrow[e]);
-                    d.cflag[pc] = 1;
+                    pc = rank_g<K>(c, d.binom, np1);
+                    if (pc >= d.C) {
+                        err |= kErrRank;
+                    } else {
+                        uint32_t* crow = d.cand + (size_t)pc * S * rwp;
+                        for (int e = 0; e < nwords; ++e)
+                            if (wrow[e]) atomicOr(&crow[e], wrow[e]);
+                        const uint32_t bit = 1u << (pc & 31);
+                        fresh = !(atomicOr(&d.cbits[pc >> 5], bit) & bit);
+                    }
+                }
+                const unsigned b = __ballot_sync(FULL_MASK, fresh);
+                if (b) {
+                    const int leader = __ffs(b) - 1;
+                    unsigned at = 0;
+                    if (lane == leader) at = atomicAdd(&d.sync[1], (unsigned)__popc(b));
+                    at = __shfl_sync(FULL_MASK, at, leader);
+                    if (fresh) d.clist[at + __popc(b & ((1u << lane) - 1u))] = pc;
                 }
             }
-            __syncwarp();
         }
+        __syncwarp();
     }
     err = __reduce_or_sync(FULL_MASK, err);
     if (lane == 0 && err) atomicOr(d.err, err);
 }
 
-// The flagged configurations of a 32-configuration window, CPW at a time: group g takes the
-// g-th remaining flag.  Returns the group's config (valid = false when fewer remain).
-template <int G>
-__device__ __forceinline__ uint32_t take_flagged(unsigned& act, size_t base, const Lanes<G>& L,
-                                                 bool& valid) {
-    constexpr int CPW = 32 / G;
-    const unsigned pos = __fns(act, 0, L.grp + 1);
-    valid = pos < 32u;
-#pragma unroll
-    for (int i = 0; i < CPW; ++i) act &= act - 1;  // (a no-op once act is empty)
-    return valid ? (uint32_t)(base + pos) : 0u;
-}
-
-// Sparse cop turn, mark: the configurations that received candidates; their candidate rows
-// are consumed and cleared for the next push.
+// Sparse cop turn, mark: the listed candidate rows, CPW per warp at a time; each is consumed and
+// cleared (row and bitmap bit) for the next push.
 template <int G>
 __device__ CR_BODY_INLINE void cop_apply_body(const V1Dev& d, int col, int nx, unsigned wk, unsigned nwk) {
     extern __shared__ uint32_t sm[];
@@ -1402,32 +1408,31 @@ __device__ CR_BODY_INLINE void cop_apply_body(const V1Dev& d, int col, int nx, u
     const int append = d.meta[col].append;
     uint32_t* wacc = sm + (warp * CPW + L.grp) * (2 * S * rwp);
     uint32_t* wnew = wacc + S * rwp;
+    const uint32_t items = d.sync[1];
     Tally t;
-    FlagScan scan(d.cflag, d.C, wk, nwk);
-    size_t base;
-    unsigned act;
-    while (scan.next(base, act)) {
-        while (act) {
-            bool valid;
-            const uint32_t cid = take_flagged<G>(act, base, L, valid);
-            uint32_t m = 0;
-            if (valid) {
-                uint32_t* crow = d.cand + (size_t)cid * S * rwp;
-                for (int e = gl; e < S * rwp; e += G) {
-                    wacc[e] = crow[e];
-                    crow[e] = 0u;
-                }
-                if (gl == 0) d.cflag[cid] = 0;
-                if (gl < rw) m = d.marked[((size_t)col * d.C + cid) * rwp + gl];
+    const uint32_t step = nwk * (blockDim.x >> 5) * CPW;
+    for (uint32_t b0 = (wk * (blockDim.x >> 5) + warp) * CPW; b0 < items; b0 += step) {
+        const uint32_t li = b0 + L.grp;
+        const bool valid = li < items;
+        const uint32_t cid = valid ? d.clist[li] : 0u;
+        uint32_t m = 0;
+        if (valid) {
+            uint32_t* crow = d.cand + (size_t)cid * S * rwp;
+            for (int e = gl; e < S * rwp; e += G) {
+                wacc[e] = crow[e];
+                crow[e] = 0u;
             }
-            __syncwarp();
-            emit_row<G>(d, cid, valid, col, m, wacc, wnew, base_in, s_used, out_base, append, L, t);
+            if (gl == 0) atomicAnd(&d.cbits[cid >> 5], ~(1u << (cid & 31)));
+            if (gl < rw) m = d.marked[((size_t)col * d.C + cid) * rwp + gl];
         }
+        __syncwarp();
+        emit_row<G>(d, cid, valid, col, m, wacc, wnew, base_in, s_used, out_base, append, L, t);
     }
     t.flush(d, col, L.lane);
 }
 
-// Deferred robber turn (odd column below the last): (C, r, c) = 1 + (C, r, c+1), row-local.
+// Deferred robber turn (odd column below the last): (C, r, c) = 1 + (C, r, c+1), row-local,
+// over column nx's row list (each entry's flag cleared as it is taken).
 template <int G>
 __device__ CR_BODY_INLINE void direct_body(const V1Dev& d, int col, int nx, unsigned wk, unsigned nwk) {
     extern __shared__ uint32_t sm[];
@@ -1437,6 +1442,7 @@ __device__ CR_BODY_INLINE void direct_body(const V1Dev& d, int col, int nx, unsi
     const int gl = L.glane;
     const int rw = d.g.rw, rwp = d.g.rwp, S = d.S;
     const ColMeta mi = d.meta[nx];
+    if (wk == 0 && threadIdx.x == 0) d.meta[nx].clean = 1;   // every listed flag is cleared below
     if (mi.hi < mi.lo) return;
     const int base_in = mi.base;
     const int s_used = min(mi.hi - base_in + 1, S);
@@ -1444,24 +1450,23 @@ __device__ CR_BODY_INLINE void direct_body(const V1Dev& d, int col, int nx, unsi
     const int append = d.meta[col].append;
     uint32_t* wacc = sm + (warp * CPW + L.grp) * (2 * S * rwp);
     uint32_t* wnew = wacc + S * rwp;
-    const uint8_t* CR_RESTRICT fflag_in = d.fflag + (size_t)nx * d.C;
+    uint8_t* fflag_in = d.fflag + (size_t)nx * d.C;
+    const RowList rl(d, nx, mi);
     Tally t;
-    FlagScan scan(fflag_in, d.C, wk, nwk);
-    size_t base;
-    unsigned act;
-    while (scan.next(base, act)) {
-        while (act) {
-            bool valid;
-            const uint32_t cid = take_flagged<G>(act, base, L, valid);
-            uint32_t m = 0;
-            if (valid) {
-                const uint32_t* row = d.front + ((size_t)nx * d.C + cid) * S * rwp;
-                for (int e = gl; e < S * rwp; e += G) wacc[e] = e < s_used * rwp ? row[e] : 0u;
-                if (gl < rw) m = d.marked[((size_t)col * d.C + cid) * rwp + gl];
-            }
-            __syncwarp();
-            emit_row<G>(d, cid, valid, col, m, wacc, wnew, base_in, s_used, out_base, append, L, t);
+    const uint32_t step = nwk * (blockDim.x >> 5) * CPW;
+    for (uint32_t b0 = (wk * (blockDim.x >> 5) + warp) * CPW; b0 < rl.n; b0 += step) {
+        const uint32_t li = b0 + L.grp;
+        const bool valid = li < rl.n;
+        const uint32_t cid = valid ? rl.id(li) : 0u;
+        uint32_t m = 0;
+        if (valid) {
+            const uint32_t* row = d.front + ((size_t)nx * d.C + cid) * S * rwp;
+            for (int e = gl; e < S * rwp; e += G) wacc[e] = e < s_used * rwp ? row[e] : 0u;
+            if (gl == 0) fflag_in[cid] = 0;
+            if (gl < rw) m = d.marked[((size_t)col * d.C + cid) * rwp + gl];
         }
+        __syncwarp();
+        emit_row<G>(d, cid, valid, col, m, wacc, wnew, base_in, s_used, out_base, append, L, t);
     }
     t.flush(d, col, L.lane);
 }
@@ -1485,6 +1490,7 @@ __device__ CR_BODY_INLINE void and_body(const V1Dev& d, int col, unsigned wk, un
     const int gl = L.glane;
     const int n = d.g.n, rw = d.g.rw, rwp = d.g.rwp, S = d.S, cols = d.cols;
     const ColMeta mi = d.meta[0];
+    if (wk == 0 && threadIdx.x == 0) d.meta[0].clean = 1;   // every listed flag is cleared below
     if (mi.hi < mi.lo) return;
     const int out_base = d.meta[col].base;
     const int per_grp = and_group_words(S, rwp);
@@ -1492,7 +1498,7 @@ __device__ CR_BODY_INLINE void and_body(const V1Dev& d, int col, unsigned wk, un
     uint32_t* wmc = wm0 + rwp;
     uint32_t* wtouch = wmc + rwp;
     uint32_t* wnew = wtouch + rwp;
-    const uint8_t* CR_RESTRICT fflag0 = d.fflag;
+    uint8_t* fflag0 = d.fflag;
     // the row tests' graph arrays (transposed hop rows, CSR), staged in shared memory when
     // the launch left room for them; read through generic pointers either way
     const uint32_t* rp = d.g.row_ptr;
@@ -1516,13 +1522,14 @@ __device__ CR_BODY_INLINE void and_body(const V1Dev& d, int col, unsigned wk, un
     }
     const int avg_deg = max(1, (nnz + n - 1) / n);
     Tally t;
-    FlagScan scan(fflag0, d.C, wk, nwk);
-    size_t base;
-    unsigned act;
-    while (scan.next(base, act)) {
-        while (act) {
-            bool valid;
-            const uint32_t cid = take_flagged<G>(act, base, L, valid);
+    const RowList rl(d, 0, mi);
+    const uint32_t step = nwk * (blockDim.x >> 5) * CPW;
+    for (uint32_t b0 = (wk * (blockDim.x >> 5) + warp) * CPW; b0 < rl.n; b0 += step) {
+        {
+            const uint32_t li = b0 + L.grp;
+            const bool valid = li < rl.n;
+            const uint32_t cid = valid ? rl.id(li) : 0u;
+            if (valid && gl == 0) fflag0[cid] = 0;
             uint32_t* mrow = d.marked + ((size_t)col * d.C + cid) * rwp;
             const uint32_t vm = (valid && gl < rw) ? valid_mask(n, gl) : 0u;
             const uint32_t mc = (valid && gl < rw) ? mrow[gl] : 0u;
@@ -1642,7 +1649,8 @@ __device__ CR_BODY_INLINE void and_body(const V1Dev& d, int col, unsigned wk, un
             uint32_t nb = 0;
             if (need && gl < rw)
                 for (int s = 0; s < S; ++s) nb |= wnew[s * rwp + gl];
-            if (L.any(nb != 0)) {
+            const bool newrow = L.any(nb != 0);
+            if (newrow) {
                 if (gl < rw) {
                     mrow[gl] = mc | nb;
                     t.cnt += __popc(nb);
@@ -1654,6 +1662,7 @@ __device__ CR_BODY_INLINE void and_body(const V1Dev& d, int col, unsigned wk, un
                     t.rows++;
                 }
             }
+            list_append(d, col, newrow && gl == 0, cid);
             __syncwarp();
         }
     }

@@ -21,6 +21,7 @@ void launch_and(const V1Dev& d, int col, bool p1, int grid, cudaStream_t st);
 void launch_prep(const V1Dev& d, int col, int nx, int grid, cudaStream_t st);
 void launch_init(const V1Dev& d, int grid, cudaStream_t st);
 void launch_init_pass1(const V1Dev& d, int num_sms, cudaStream_t st);
+void launch_list_compact(const V1Dev& d, int col, int num_sms, cudaStream_t st);
 void launch_marks_from_table(const uint8_t* table, uint32_t C, int n, int cols, int rwp, uint32_t* marked,
                              int grid, cudaStream_t st);
 void launch_game(const uint8_t* table, const uint16_t* configs, const unsigned long long* heads,
@@ -655,8 +656,8 @@ static int v1_init_pass1(cr_solver* s, uint64_t* found) {
     cudaStream_t st = ctx->stream;
     CR_CUDA(ctx, cudaMemsetAsync(s->d_counters, 0, 4 * sizeof(unsigned long long), st));
     CR_CUDA(ctx, cudaMemsetAsync(s->d_err, 0, sizeof(unsigned), st));
-    // column 0's frontier after pass 1 is every row (the implicit list), column 1's the rows
-    // the kernel lists
+    // column 0's frontier after pass 1 is every row (the implicit list); column 1's list is
+    // built from its flags after the kernel
     ColMeta meta[2] = {ColMeta{0, 0, 0, 0, (int)std::min<uint64_t>(s->C, INT32_MAX), 0, -1, 0},
                        ColMeta{1, kEmptyLo, -1, 0, 0, 0, 0, 0}};
     CR_CUDA(ctx, cudaMemsetAsync(s->d_sync, 0, 2 * sizeof(unsigned), st));
@@ -666,13 +667,15 @@ static int v1_init_pass1(cr_solver* s, uint64_t* found) {
     launch_init_pass1(d, ctx->num_sms, st);
     CR_CUDA(ctx, cudaGetLastError());
     CR_CUDA(ctx, cudaEventRecord(s->evc1, st));
+    launch_list_compact(d, 1, ctx->num_sms, st);   // column 1's row list, from its flags
+    CR_CUDA(ctx, cudaGetLastError());
     CR_CUDA(ctx, cudaMemcpyAsync(s->h_pinned, s->d_counters, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     CR_CUDA(ctx, cudaStreamSynchronize(st));
     float ms = 0;
     cudaEventElapsedTime(&ms, s->evc0, s->evc1);
     s->stats.init_ms = ms;
     s->init_pending = false;
-    s->stats.kernel_launches += 1;
+    s->stats.kernel_launches += 2;
     *found = s->h_pinned[0];
     return CR_OK;
 }

@@ -311,6 +311,59 @@ void launch_init_pass1(const V1Dev& d, int num_sms, cudaStream_t st) {
     else launch_init_pass1_s<false>(d, grid, 0, st);
 }
 
+// Builds column col's row list from its flag plane (after the first pass): each block takes
+// segments of 16 flags per thread, counts the set ones, reserves its segment's room in the list
+// with one atomic and writes the ids (the list order is irrelevant to its consumers).
+__global__ void __launch_bounds__(256) k_list_compact(V1Dev d, int col) {
+    __shared__ unsigned s_warp[8];
+    __shared__ unsigned s_at;
+    constexpr int kPer = 16;
+    const uint8_t* f = d.fflag + (size_t)col * d.C;
+    uint32_t* out = d.list + (size_t)col * d.C;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const size_t seg = (size_t)blockDim.x * kPer;
+    for (size_t base = (size_t)blockIdx.x * seg; base < d.C; base += (size_t)gridDim.x * seg) {
+        unsigned bits = 0;   // bit j: flag base + j * blockDim.x + threadIdx.x is set
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            const size_t i = base + (size_t)j * blockDim.x + threadIdx.x;
+            if (i < d.C && f[i]) bits |= 1u << j;
+        }
+        const unsigned mine = __popc(bits);
+        unsigned incl = mine;   // inclusive scan over the warp
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        if (lane == 31) s_warp[warp] = incl;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned tot = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+                const unsigned c = s_warp[w];
+                s_warp[w] = tot;
+                tot += c;
+            }
+            s_at = tot ? (unsigned)atomicAdd(&d.meta[col].len, (int)tot) : 0u;
+        }
+        __syncthreads();
+        unsigned at = s_at + s_warp[warp] + incl - mine;
+        while (bits) {
+            const int j = __ffs(bits) - 1;
+            bits &= bits - 1;
+            out[at++] = (uint32_t)(base + (size_t)j * blockDim.x + threadIdx.x);
+        }
+        __syncthreads();
+    }
+}
+
+void launch_list_compact(const V1Dev& d, int col, int num_sms, cudaStream_t st) {
+    const uint64_t segs = ((uint64_t)d.C + 256 * 16 - 1) / (256 * 16);
+    const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(segs, (uint64_t)num_sms * 4));
+    k_list_compact<<<grid, 256, 0, st>>>(d, col);
+}
+
 void launch_verdict(const V1Dev& d, int cols, unsigned long long* best, int grid, cudaStream_t st) {
     k_verdict<<<grid, 256, 0, st>>>(d.table, d.marked, d.C, d.g.n, d.g.rw, d.g.rwp, cols, best);
 }

@@ -52,26 +52,87 @@ __device__ __forceinline__ bool frontier_sparse(const ColMeta& m, uint32_t C) {
     return (unsigned long long)m.rows * kPushRatio < C;
 }
 
-// Per-warp running totals a producer reports once at the end of its grid-stride loop.
+// A warp's buffer of row ids bound for a column's list: up to 32 ids, one per lane, written out
+// with one atomic on the list length when full and at the end (appends from every warp of a
+// grid would otherwise serialise on that one counter, and a returning atomic per append puts
+// its latency on the warp's path).
+struct ListBuf {
+    uint32_t lbuf = 0;
+    int lcount = 0;   // warp-uniform
+
+    __device__ __forceinline__ void spill(const V1Dev& d, int col, int lane) {
+        int at = 0;
+        if (lane == 0) at = atomicAdd(&d.meta[col].len, lcount);
+        at = __shfl_sync(FULL_MASK, at, 0);
+        if (lane < lcount) d.list[(size_t)col * d.C + at + lane] = lbuf;
+        lcount = 0;
+    }
+    // Appends id for every lane whose pred is set (warp-collective).
+    __device__ __forceinline__ void append(const V1Dev& d, int col, bool pred, uint32_t id, int lane) {
+        const unsigned b = __ballot_sync(FULL_MASK, pred);
+        if (!b) return;
+        const int k = __popc(b);
+        if (lcount + k > 32) spill(d, col, lane);
+        // lane lcount + j takes the id of the j-th lane with pred set
+        const bool dst = lane >= lcount && lane < lcount + k;
+        const int src = dst ? (int)__fns(b, 0, lane - lcount + 1) : lane;
+        const uint32_t v = __shfl_sync(FULL_MASK, id, src);
+        if (dst) lbuf = v;
+        lcount += k;
+    }
+    __device__ __forceinline__ void finish(const V1Dev& d, int col, int lane) {
+        if (lcount) spill(d, col, lane);
+    }
+};
+
+// Running totals of a producer (count of new marks, listed rows, value range, error bits) and
+// its list buffer.  flush() empties the buffer and reduces the totals over the block, so a
+// block reports with one atomic per field; every thread of the block calls it once, at the end
+// of the body.
 struct Tally {
     unsigned cnt = 0, err = 0, rows = 0;
     int lo = kEmptyLo, hi = -1;
+    ListBuf lb;
 
+    __device__ __forceinline__ void append(const V1Dev& d, int col, bool pred, uint32_t id, int lane) {
+        lb.append(d, col, pred, id, lane);
+    }
     __device__ void flush(const V1Dev& d, int col, int lane) {
+        lb.finish(d, col, lane);
+        __shared__ unsigned s_u[3][32];
+        __shared__ int s_i[2][32];
+        const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
         cnt = __reduce_add_sync(FULL_MASK, cnt);
         rows = __reduce_add_sync(FULL_MASK, rows);
         lo = __reduce_min_sync(FULL_MASK, lo);
         hi = __reduce_max_sync(FULL_MASK, hi);
         err = __reduce_or_sync(FULL_MASK, err);
         if (lane == 0) {
-            if (cnt) atomicAdd(d.pass_new, (unsigned long long)cnt);
-            if (rows) atomicAdd(&d.meta[col].rows, (int)rows);
-            if (hi >= 0) {
-                atomicMin(&d.meta[col].lo, lo);
-                atomicMax(&d.meta[col].hi, hi);
-            }
-            if (err) atomicOr(d.err, err);
+            s_u[0][w] = cnt;
+            s_u[1][w] = rows;
+            s_u[2][w] = err;
+            s_i[0][w] = lo;
+            s_i[1][w] = hi;
         }
+        __syncthreads();
+        if (w == 0) {
+            const bool in = lane < nw;
+            cnt = __reduce_add_sync(FULL_MASK, in ? s_u[0][lane] : 0u);
+            rows = __reduce_add_sync(FULL_MASK, in ? s_u[1][lane] : 0u);
+            err = __reduce_or_sync(FULL_MASK, in ? s_u[2][lane] : 0u);
+            lo = __reduce_min_sync(FULL_MASK, in ? s_i[0][lane] : kEmptyLo);
+            hi = __reduce_max_sync(FULL_MASK, in ? s_i[1][lane] : -1);
+            if (lane == 0) {
+                if (cnt) atomicAdd(d.pass_new, (unsigned long long)cnt);
+                if (rows) atomicAdd(&d.meta[col].rows, (int)rows);
+                if (hi >= 0) {
+                    atomicMin(&d.meta[col].lo, lo);
+                    atomicMax(&d.meta[col].hi, hi);
+                }
+                if (err) atomicOr(d.err, err);
+            }
+        }
+        __syncthreads();
     }
 };
 
@@ -115,18 +176,6 @@ __device__ CR_BODY_INLINE void prep_body(const V1Dev& d, int col, int nx, unsign
             if (col == d.cols - 1) d.meta[0].append = 0;   // column 0's seeded frontier is consumed
         }
     }
-}
-
-// Appends `id` to column col's row list for every lane whose pred is set (warp-collective:
-// every lane of the warp calls it; one atomic per warp).
-__device__ __forceinline__ void list_append(const V1Dev& d, int col, bool pred, uint32_t id) {
-    const unsigned b = __ballot_sync(FULL_MASK, pred);
-    if (!b) return;
-    const int lane = threadIdx.x & 31, leader = __ffs(b) - 1;
-    int at = 0;
-    if (lane == leader) at = atomicAdd(&d.meta[col].len, __popc(b));
-    at = __shfl_sync(FULL_MASK, at, leader);
-    if (pred) d.list[(size_t)col * d.C + at + __popc(b & ((1u << lane) - 1u))] = id;
 }
 
 // The row list of a column's frontier as a consumer sees it: n entries, entry i = row id(i).
@@ -307,7 +356,9 @@ __device__ __forceinline__ void next_multiset(int (&c)[K], int n) {
 // owns robbers 8l .. 8l+7 of each 256-vertex block, i.e. one 16-byte piece of the row, and
 // the 8-bit pieces of the marked and frontier rows, which four lanes assemble into a word.
 // The caller sets meta[0] = {0, 0, 0, 0, C, 0}, meta[1] = {1, empty, -1, 0, 0, 0} and zeroes
-// the pass counter; the pass counter then holds the first pass's count.
+// the pass counter; the pass counter then holds the first pass's count.  Column 0's list is the
+// implicit one (every row); column 1's is built from its flags afterwards (list_compact), which
+// keeps list atomics off the warps that own the rare column-1 rows.
 // The same sweep for rows of one 256-robber block whose robbers split into whole lane pieces
 // (n <= 256, n a multiple of 8), organised around the common configuration.  Consecutive
 // configurations share their leading cops c[0 .. K-2] for a run of up to n of them (only the
@@ -537,7 +588,6 @@ __device__ CR_BODY_INLINE void init_pass1_single(const V1Dev& d, unsigned wk, un
                     d.fflag[(size_t)C + id] = 1;
                     ++rows1;
                 }
-                list_append(d, 1, lane == 0, (uint32_t)id);
             }
             uint32_t* m0row = marked + id * rwp;
             uint32_t* m1row = marked + ((size_t)C + id) * rwp;
@@ -770,7 +820,6 @@ __device__ CR_BODY_INLINE void init_pass1_body(const V1Dev& d, unsigned wk, unsi
             *fl1 = changed ? 1 : 0;
             rows1 += changed ? 1u : 0u;
         }
-        list_append(d, 1, lane == 0 && changed, (uint32_t)cid);
     }
     cnt = __reduce_add_sync(FULL_MASK, cnt);
     rows1 = __reduce_add_sync(FULL_MASK, rows1);
@@ -873,7 +922,7 @@ __device__ __forceinline__ void emit_row(const V1Dev& d, uint32_t cid, bool vali
         }
     }
     // (in append mode every row is already listed: the list is the implicit one)
-    list_append(d, col, newrow && gl == 0 && !append, cid);
+    t.append(d, col, newrow && gl == 0 && !append, cid, L.lane);
     __syncwarp();
 }
 
@@ -1662,7 +1711,7 @@ __device__ CR_BODY_INLINE void and_body(const V1Dev& d, int col, unsigned wk, un
                     t.rows++;
                 }
             }
-            list_append(d, col, newrow && gl == 0, cid);
+            t.append(d, col, newrow && gl == 0, cid, L.lane);
             __syncwarp();
         }
     }

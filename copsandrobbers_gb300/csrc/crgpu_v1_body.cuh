@@ -141,7 +141,8 @@ struct Tally {
 // clear each row's flag as they take it; the dense cop turns read flags at random and leave
 // them), then fix the value base of the new frontier and empty its range and list -- unless
 // the column is in append mode (column 0 in pass 1 after the unfused initializeCaptures, whose
-// frontier already holds the capture seeds).  Every block reads the column's state first; the
+// frontier already holds the capture seeds).  Before an odd column it also clears the candidate
+// rows of the push-mode cop turn just run.  Every block reads the column's state first; the
 // last block to finish (counted in sync[0]) resets it, so no block reads a half-reset state.
 __device__ CR_BODY_INLINE void prep_body(const V1Dev& d, int col, int nx, unsigned wk, unsigned nwk) {
     ColMeta* mo = d.meta + col;
@@ -150,6 +151,16 @@ __device__ CR_BODY_INLINE void prep_body(const V1Dev& d, int col, int nx, unsign
         uint8_t* f = d.fflag + (size_t)col * d.C;
         for (size_t i = (size_t)wk * blockDim.x + threadIdx.x; i < d.C; i += (size_t)nwk * blockDim.x)
             f[i] = 0;
+    }
+    if (col % 2 == 1) {
+        // the candidate rows (and their bitmap words) the cop turn into column col - 1 consumed
+        const size_t words = (size_t)d.S * d.g.rwp, total = (size_t)d.sync[1] * words;
+        for (size_t i = (size_t)wk * blockDim.x + threadIdx.x; i < total; i += (size_t)nwk * blockDim.x) {
+            const uint32_t cid = d.clist[i / words];
+            const size_t e = i % words;
+            d.cand[(size_t)cid * words + e] = 0u;
+            if (e == 0) d.cbits[cid >> 5] = 0u;
+        }
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1439,8 +1450,9 @@ __device__ CR_BODY_INLINE void cop_push_body(const V1Dev& d, int col, int nx, un
     if (lane == 0 && err) atomicOr(d.err, err);
 }
 
-// Sparse cop turn, mark: the listed candidate rows, CPW per warp at a time; each is consumed and
-// cleared (row and bitmap bit) for the next push.
+// Sparse cop turn, mark: the listed candidate rows, CPW per warp at a time.  The rows and their
+// bitmap bits are cleared for the next push by the following prep (write-only stores there;
+// zeroing each row right after reading it here cost six times the reads).
 template <int G>
 __device__ CR_BODY_INLINE void cop_apply_body(const V1Dev& d, int col, int nx, unsigned wk, unsigned nwk) {
     extern __shared__ uint32_t sm[];
@@ -1466,12 +1478,8 @@ __device__ CR_BODY_INLINE void cop_apply_body(const V1Dev& d, int col, int nx, u
         const uint32_t cid = valid ? d.clist[li] : 0u;
         uint32_t m = 0;
         if (valid) {
-            uint32_t* crow = d.cand + (size_t)cid * S * rwp;
-            for (int e = gl; e < S * rwp; e += G) {
-                wacc[e] = crow[e];
-                crow[e] = 0u;
-            }
-            if (gl == 0) atomicAnd(&d.cbits[cid >> 5], ~(1u << (cid & 31)));
+            const uint32_t* crow = d.cand + (size_t)cid * S * rwp;
+            for (int e = gl; e < S * rwp; e += G) wacc[e] = crow[e];
             if (gl < rw) m = d.marked[((size_t)col * d.C + cid) * rwp + gl];
         }
         __syncwarp();

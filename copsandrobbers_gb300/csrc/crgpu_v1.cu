@@ -23,14 +23,15 @@
 // The frontier of a column is split into value slots (one bit plane per value) so that the
 // cop-turn minimum is a sequence of bitwise ORs: the lowest slot with a bit gives the value.
 //
-// The cop turn runs in one of two forms chosen on the device from the frontier's row count:
-//   seed          the capture seeds of column 1 before pass 1, in closed form (k_cop_seed);
-//   pull (dense)  every configuration ORs the frontier rows of its successors (k_cop_pull);
-//   push (sparse) every non-empty frontier row is ORed into the candidate rows of its
-//                 predecessors with atomics (k_cop_push), then only those are marked
-//                 (k_cop_apply).
-// The capture seeds (the frontier of column 1 before pass 1) have a closed form: the OR of
-// the seed rows over T(C) is the union of the cops' neighbourhoods.
+// The cop turn runs in one of these forms, chosen on the device from the frontier's row count:
+//   seed          the capture seeds of column 1 before pass 1, in closed form: the OR of the
+//                 seed rows over T(C) is the union of the cops' neighbourhoods;
+//   pull (dense)  every configuration ORs the frontier rows of its successors (k_cop_pull), or
+//                 for k = 3 in separable form through pair rows (pair_h1 + sep_pull);
+//   push (sparse) every row of the frontier's list is ORed into the candidate rows of its
+//                 predecessors with atomics, then only those rows are marked (push + apply).
+// k_cop_a and k_cop_b carry the seed, push, apply and separable bodies (each body returns at
+// once unless its form applies), so a cop turn is two launches for k = 3 and three otherwise.
 #include "crgpu_internal.cuh"
 
 #include <algorithm>
@@ -64,26 +65,21 @@ template <int K, int NWP, int G>
 __global__ void __launch_bounds__(256) k_cop_pull(V1Dev d, int col, int nx) {
     cop_pull_body<K, NWP, G>(d, col, nx, blockIdx.x, gridDim.x);
 }
-// The separable cop turn is latency-bound too: at most 64 registers (4 blocks of 256 per SM),
-// or 80 (3 blocks) for 32-word rows, whose accumulators do not fit in 64 without spilling.
-template <int NWP, int G>
-__global__ void __launch_bounds__(256, NWP >= 32 ? 3 : 4) k_pair_h1(V1Dev d, int nx) {
-    pair_h1_body<NWP, G>(d, nx, blockIdx.x, gridDim.x);
-}
-template <int NWP, int G>
-__global__ void __launch_bounds__(256, NWP >= 32 ? 3 : 4) k_sep_pull(V1Dev d, int col, int nx) {
-    sep_pull_body<NWP, G>(d, col, nx, blockIdx.x, gridDim.x);
-}
-template <int K, int G>
-__global__ void __launch_bounds__(256) k_cop_seed(V1Dev d, int col, int nx) {
+// The other cop-turn forms share two launches, each body returning at once unless its form
+// applies (the form is chosen on the device from the input frontier):
+//   k_cop_a  the capture-seed form, the push scatter, or (k = 3) the separable turn's pair rows;
+//   k_cop_b  the separable turn's configurations (k = 3) or the push form's marking.
+// The tuple-gathering pull (k != 3, or no pair rows) keeps its own launch: it wants up to 127
+// registers, the bodies here at most 64 (80 with 32-word rows), being latency-bound.
+template <int K, int NWP, int G>
+__global__ void __launch_bounds__(256, NWP >= 32 ? 3 : 4) k_cop_a(V1Dev d, int col, int nx) {
     cop_seed_body<K, G>(d, col, nx, blockIdx.x, gridDim.x);
-}
-template <int K>
-__global__ void __launch_bounds__(256) k_cop_push(V1Dev d, int col, int nx) {
     cop_push_body<K>(d, col, nx, blockIdx.x, gridDim.x);
+    if constexpr (K == 3) pair_h1_body<NWP, G>(d, nx, blockIdx.x, gridDim.x);
 }
-template <int G>
-__global__ void __launch_bounds__(256) k_cop_apply(V1Dev d, int col, int nx) {
+template <int K, int NWP, int G>
+__global__ void __launch_bounds__(256, NWP >= 32 ? 3 : 4) k_cop_b(V1Dev d, int col, int nx) {
+    if constexpr (K == 3) sep_pull_body<NWP, G>(d, col, nx, blockIdx.x, gridDim.x);
     cop_apply_body<G>(d, col, nx, blockIdx.x, gridDim.x);
 }
 template <int G>
@@ -143,97 +139,51 @@ static int pull_words(int S, int rwp) {
 
 bool pull_supported(int S, int rwp) { return pull_words(S, rwp) <= 32 && group_lanes(rwp) <= 32; }
 
-template <int K, int G>
-static void launch_pull_g(const V1Dev& d, int col, int nx, int grid, cudaStream_t st) {
-    const size_t sm = cop_smem_bytes(d.S, d.g.rwp) + (size_t)rank_table_words(K, d.g.n) * 4;
-    switch (pull_words(d.S, d.g.rwp)) {
-        case 2: if (G == 4) k_cop_pull<K, 2, 4><<<grid, 256, sm, st>>>(d, col, nx); break;
-        case 4: if (G == 4) k_cop_pull<K, 4, 4><<<grid, 256, sm, st>>>(d, col, nx); break;
-        case 8: if (G == 4) k_cop_pull<K, 8, 4><<<grid, 256, sm, st>>>(d, col, nx); break;
-        case 16:
-            if (G == 4) k_cop_pull<K, 16, 4><<<grid, 256, sm, st>>>(d, col, nx);
-            else k_cop_pull<K, 16, 8><<<grid, 256, sm, st>>>(d, col, nx);
-            break;
-        default:
-            if (G == 4) k_cop_pull<K, 32, 4><<<grid, 256, sm, st>>>(d, col, nx);
-            else if (G == 8) k_cop_pull<K, 32, 8><<<grid, 256, sm, st>>>(d, col, nx);
-            else k_cop_pull<K, 32, 16><<<grid, 256, sm, st>>>(d, col, nx);
-            break;
-    }
-}
-
-template <int NWP, int G>
-static void launch_sep_ng(const V1Dev& d, int col, int nx, int grid, cudaStream_t st) {
+template <int K, int NWP, int G>
+static void launch_cop_ng(const V1Dev& d, int col, int nx, int grid, cudaStream_t st) {
     const size_t sm = cop_smem_bytes(d.S, d.g.rwp);
-    k_pair_h1<NWP, G><<<grid, 256, sm + (size_t)rank_table_words(3, d.g.n) * 4, st>>>(d, nx);
-    k_sep_pull<NWP, G><<<grid, 256, sm, st>>>(d, col, nx);
+    const size_t smr = sm + (size_t)rank_table_words(K, d.g.n) * 4;
+    k_cop_a<K, NWP, G><<<grid, 256, smr, st>>>(d, col, nx);
+    if (!(K == 3 && d.h1)) k_cop_pull<K, NWP, G><<<grid, 256, smr, st>>>(d, col, nx);
+    k_cop_b<K, NWP, G><<<grid, 256, sm, st>>>(d, col, nx);
 }
 
-// The separable k = 3 dense cop turn (same word and lane shapes as the pull).
-template <int G>
-static void launch_sep_g(const V1Dev& d, int col, int nx, int grid, cudaStream_t st) {
-    switch (pull_words(d.S, d.g.rwp)) {
-        case 2: if (G == 4) launch_sep_ng<2, 4>(d, col, nx, grid, st); break;
-        case 4: if (G == 4) launch_sep_ng<4, 4>(d, col, nx, grid, st); break;
-        case 8: if (G == 4) launch_sep_ng<8, 4>(d, col, nx, grid, st); break;
-        case 16:
-            if (G == 4) launch_sep_ng<16, 4>(d, col, nx, grid, st);
-            else launch_sep_ng<16, 8>(d, col, nx, grid, st);
-            break;
-        default:
-            if (G == 4) launch_sep_ng<32, 4>(d, col, nx, grid, st);
-            else if (G == 8) launch_sep_ng<32, 8>(d, col, nx, grid, st);
-            else launch_sep_ng<32, 16>(d, col, nx, grid, st);
-            break;
-    }
-}
-
-template <int G>
-static void launch_rows_g(const V1Dev& d, int col, int nx, int direct, int grid, cudaStream_t st) {
-    const size_t sm = cop_smem_bytes(d.S, d.g.rwp);
-    if (direct) k_direct<G><<<grid, 256, sm, st>>>(d, col, nx);
-    else k_cop_apply<G><<<grid, 256, sm, st>>>(d, col, nx);
-}
-
-static void launch_rows(const V1Dev& d, int col, int nx, int direct, int grid, cudaStream_t st) {
-    switch (group_lanes(d.g.rwp)) {
-        case 4: launch_rows_g<4>(d, col, nx, direct, grid, st); break;
-        case 8: launch_rows_g<8>(d, col, nx, direct, grid, st); break;
-        case 16: launch_rows_g<16>(d, col, nx, direct, grid, st); break;
-        default: launch_rows_g<32>(d, col, nx, direct, grid, st); break;
-    }
-}
-
+// Accumulator words and lanes per configuration, as the pull and the separable turn use them.
 template <int K>
 static void launch_cop_k(const V1Dev& d, int col, int nx, int grid, cudaStream_t st) {
-    const size_t sm = cop_smem_bytes(d.S, d.g.rwp);
-    switch (group_lanes(d.g.rwp)) {
-        case 4: k_cop_seed<K, 4><<<grid, 256, sm, st>>>(d, col, nx); break;
-        case 8: k_cop_seed<K, 8><<<grid, 256, sm, st>>>(d, col, nx); break;
-        case 16: k_cop_seed<K, 16><<<grid, 256, sm, st>>>(d, col, nx); break;
-        default: k_cop_seed<K, 32><<<grid, 256, sm, st>>>(d, col, nx); break;
+    const int G = group_lanes(d.g.rwp);
+    switch (pull_words(d.S, d.g.rwp)) {
+        case 2: launch_cop_ng<K, 2, 4>(d, col, nx, grid, st); break;
+        case 4: launch_cop_ng<K, 4, 4>(d, col, nx, grid, st); break;
+        case 8: launch_cop_ng<K, 8, 4>(d, col, nx, grid, st); break;
+        case 16:
+            if (G == 4) launch_cop_ng<K, 16, 4>(d, col, nx, grid, st);
+            else launch_cop_ng<K, 16, 8>(d, col, nx, grid, st);
+            break;
+        default:
+            if (G == 4) launch_cop_ng<K, 32, 4>(d, col, nx, grid, st);
+            else if (G == 8) launch_cop_ng<K, 32, 8>(d, col, nx, grid, st);
+            else launch_cop_ng<K, 32, 16>(d, col, nx, grid, st);
+            break;
     }
-    switch (group_lanes(d.g.rwp)) {
-        case 4: launch_pull_g<K, 4>(d, col, nx, grid, st); break;
-        case 8: launch_pull_g<K, 8>(d, col, nx, grid, st); break;
-        default: launch_pull_g<K, 16>(d, col, nx, grid, st); break;
-    }
-    if (K == 3 && d.h1) {
-        switch (group_lanes(d.g.rwp)) {
-            case 4: launch_sep_g<4>(d, col, nx, grid, st); break;
-            case 8: launch_sep_g<8>(d, col, nx, grid, st); break;
-            default: launch_sep_g<16>(d, col, nx, grid, st); break;
-        }
-    }
-    k_cop_push<K><<<grid, 256, (size_t)8 * d.S * d.g.rwp * 4, st>>>(d, col, nx);
-    launch_rows(d, col, nx, 0, grid, st);
 }
 
-// Cop turn into column col: the pull kernel and the push pair are all enqueued; each reads
-// the input frontier's row count on the device and only the matching form does work.
+template <int G>
+static void launch_direct_g(const V1Dev& d, int col, int nx, int grid, cudaStream_t st) {
+    k_direct<G><<<grid, 256, cop_smem_bytes(d.S, d.g.rwp), st>>>(d, col, nx);
+}
+
+// Cop turn into column col (or, direct = 1, a deferred robber turn): every form that may apply
+// is enqueued; each reads the input frontier's row count on the device and only the matching
+// form does work.
 void launch_cop(const V1Dev& d, int col, int nx, int direct, int grid, cudaStream_t st) {
     if (direct) {
-        launch_rows(d, col, nx, 1, grid, st);
+        switch (group_lanes(d.g.rwp)) {
+            case 4: launch_direct_g<4>(d, col, nx, grid, st); break;
+            case 8: launch_direct_g<8>(d, col, nx, grid, st); break;
+            case 16: launch_direct_g<16>(d, col, nx, grid, st); break;
+            default: launch_direct_g<32>(d, col, nx, grid, st); break;
+        }
         return;
     }
     switch (d.k) {
@@ -244,8 +194,8 @@ void launch_cop(const V1Dev& d, int col, int nx, int direct, int grid, cudaStrea
     }
 }
 
-int cop_launches(int direct) { return direct ? 1 : 4; }
-int cop_launches_k(int direct, int k, bool sep) { return direct ? 1 : (k == 3 && sep ? 6 : 4); }
+int cop_launches(int direct) { return direct ? 1 : 3; }
+int cop_launches_k(int direct, int k, bool sep) { return direct ? 1 : (k == 3 && sep ? 2 : 3); }
 
 // Shared-memory words the last-column body stages the graph in: transposed hop rows, row
 // pointers and neighbour lists.

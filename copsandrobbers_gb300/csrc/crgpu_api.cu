@@ -28,6 +28,8 @@ void launch_game(const uint8_t* table, const uint16_t* configs, const unsigned l
                  const unsigned long long* trans, const uint32_t* rp, const uint16_t* adj, int n, int k,
                  long long best, int cap, long long* out_c, int* out_r, int* count, int* captured,
                  cudaStream_t st);
+void launch_loop_start(const unsigned long long* counters, unsigned long long* hist, const int* idx,
+                       const unsigned* err, cudaGraphConditionalHandle loop, cudaStream_t st);
 void launch_pass_end(const unsigned long long* counters, unsigned long long* hist, int* idx, int cap,
                      const unsigned* err, cudaGraphConditionalHandle loop, cudaStream_t st);
 void launch_verdict(const V1Dev& d, int cols, unsigned long long* best, int grid, cudaStream_t st);
@@ -96,7 +98,9 @@ struct cr_solver {
     unsigned long long* d_heads = nullptr;
     unsigned long long* d_trans = nullptr;
     uint64_t n_trans = 0;
-    unsigned long long* h_pinned = nullptr;  // pinned read-back slot for the pass counter
+    // pinned read-back slots: [0..3] counters, [4..4+kPinHist) the pass history, then its
+    // length and the error bits
+    unsigned long long* h_pinned = nullptr;
     cudaGraphExec_t pass_graph = nullptr;
     // mainLoop on the device: a graph whose WHILE node replays one pass until a pass finds
     // nothing; the pass counts land in d_hist, their number in d_hist_n
@@ -140,6 +144,8 @@ static int fail(cr_context* ctx, int code, const char* fmt, ...) {
         if (e_ != cudaSuccess)                                                              \
             return fail((ctx), CR_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
     } while (0)
+
+static constexpr int kPinHist = 64;   // pass counts read back with the pass loop's end
 
 static uint64_t binom_u64(int64_t n, int64_t k) {
     if (k < 0 || n < 0 || k > n) return 0;
@@ -559,7 +565,7 @@ int cr_solver_create(cr_context* ctx, const cr_graph* g, int32_t k, int32_t p, i
     CR_TRY(cudaMalloc(&s->d_configs, s->C * k * 2));
     CR_TRY(cudaMalloc(&s->d_counters, 4 * sizeof(unsigned long long)));
     CR_TRY(cudaMalloc(&s->d_err, sizeof(unsigned int)));
-    CR_TRY(cudaMallocHost(&s->h_pinned, 4 * sizeof(unsigned long long)));
+    CR_TRY(cudaMallocHost(&s->h_pinned, (4 + kPinHist + 1) * sizeof(unsigned long long)));
     CR_TRY(cudaEventCreate(&s->ev0));
     CR_TRY(cudaEventCreate(&s->ev1));
     CR_TRY(cudaEventCreate(&s->evc0));
@@ -651,7 +657,7 @@ static int v1_init(cr_solver* s, uint64_t* caps) {
 // initializeCaptures and pass 1 of a p = 1 solve in one kernel (init_pass1_single /
 // init_pass1_body): every table byte, both marked planes and both flag planes are written whole
 // (column 1's frontier rows where they gained marks), so nothing is cleared first.
-static int v1_init_pass1(cr_solver* s, uint64_t* found) {
+static int v1_init_pass1_enqueue(cr_solver* s) {
     cr_context* ctx = s->ctx;
     cudaStream_t st = ctx->stream;
     CR_CUDA(ctx, cudaMemsetAsync(s->d_counters, 0, 4 * sizeof(unsigned long long), st));
@@ -669,13 +675,24 @@ static int v1_init_pass1(cr_solver* s, uint64_t* found) {
     CR_CUDA(ctx, cudaEventRecord(s->evc1, st));
     launch_list_compact(d, 1, ctx->num_sms, st);   // column 1's row list, from its flags
     CR_CUDA(ctx, cudaGetLastError());
-    CR_CUDA(ctx, cudaMemcpyAsync(s->h_pinned, s->d_counters, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-    CR_CUDA(ctx, cudaStreamSynchronize(st));
+    s->init_pending = false;
+    s->stats.kernel_launches += 2;
+    return CR_OK;
+}
+
+static void v1_init_pass1_time(cr_solver* s) {
     float ms = 0;
     cudaEventElapsedTime(&ms, s->evc0, s->evc1);
     s->stats.init_ms = ms;
-    s->init_pending = false;
-    s->stats.kernel_launches += 2;
+}
+
+static int v1_init_pass1(cr_solver* s, uint64_t* found) {
+    cr_context* ctx = s->ctx;
+    cudaStream_t st = ctx->stream;
+    if (int rc = v1_init_pass1_enqueue(s)) return rc;
+    CR_CUDA(ctx, cudaMemcpyAsync(s->h_pinned, s->d_counters, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    CR_CUDA(ctx, cudaStreamSynchronize(st));
+    v1_init_pass1_time(s);
     *found = s->h_pinned[0];
     return CR_OK;
 }
@@ -859,7 +876,8 @@ int cr_solver_pass(cr_solver* s, uint64_t* new_wins) {
 
 static constexpr int kHistCap = 1 << 16;   // passes one device-side loop may run
 
-// The pass loop graph: WHILE (flag) { one pass; k_pass_end }, the flag set by k_pass_end.
+// The pass loop graph: k_loop_start; WHILE (flag) { one pass; k_pass_end }, the flag set by
+// k_loop_start and then by each k_pass_end.
 static int build_run_graph(cr_solver* s) {
     cr_context* ctx = s->ctx;
     cudaStream_t st = ctx->stream;
@@ -870,14 +888,25 @@ static int build_run_graph(cr_solver* s) {
     cudaGraph_t g = nullptr;
     CR_CUDA(ctx, cudaGraphCreate(&g, 0));
     cudaGraphConditionalHandle loop;
-    cudaError_t e = cudaGraphConditionalHandleCreate(&loop, g, 1, cudaGraphCondAssignDefault);
+    cudaError_t e = cudaGraphConditionalHandleCreate(&loop, g, 0, cudaGraphCondAssignDefault);
+    // the start node sets the loop condition (and records a first pass run just before)
+    cudaGraphNode_t start = nullptr;
+    if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(st, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        launch_loop_start(s->d_counters, s->d_hist, s->d_hist_n, s->d_err, loop, st);
+        cudaGraph_t same = nullptr;
+        e = cudaStreamEndCapture(st, &same);
+    }
+    size_t nodes = 1;
+    if (e == cudaSuccess) e = cudaGraphGetNodes(g, &start, &nodes);
+    if (e == cudaSuccess && nodes != 1) e = cudaErrorInvalidValue;
     cudaGraphNodeParams cp = {};
     cp.type = cudaGraphNodeTypeConditional;
     cp.conditional.handle = loop;
     cp.conditional.type = cudaGraphCondTypeWhile;
     cp.conditional.size = 1;
     cudaGraphNode_t node;
-    if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp);
+    if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, &start, nullptr, 1, &cp);
     if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(st, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
                                                             cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
@@ -909,25 +938,41 @@ static int v1_run_on_device(cr_solver* s) {
         int rc = build_run_graph(s);
         if (rc) return rc;
     }
-    CR_CUDA(ctx, cudaMemsetAsync(s->d_hist_n, 0, sizeof(int), st));
+    // p = 1: the fused first pass is enqueued right before the loop, whose start node records
+    // its count, so the whole solve costs one host synchronisation
+    const bool first = s->init_pending;
     CR_CUDA(ctx, cudaEventRecord(s->ev0, st));
+    if (first) {
+        if (int rc = v1_init_pass1_enqueue(s)) return rc;
+    }
+    CR_CUDA(ctx, cudaMemsetAsync(s->d_hist_n, 0, sizeof(int), st));
+    if (first) CR_CUDA(ctx, cudaMemsetAsync(s->d_hist_n, 1, 1, st));   // the length 1 (low byte)
     CR_CUDA(ctx, cudaGraphLaunch(s->run_graph, st));
     CR_CUDA(ctx, cudaEventRecord(s->ev1, st));
-    int n = 0;
-    unsigned bits = 0;
-    CR_CUDA(ctx, cudaMemcpyAsync(&n, s->d_hist_n, sizeof(int), cudaMemcpyDeviceToHost, st));
-    CR_CUDA(ctx, cudaMemcpyAsync(&bits, s->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    unsigned long long* hist_pin = s->h_pinned + 4;
+    unsigned* tail = reinterpret_cast<unsigned*>(s->h_pinned + 4 + kPinHist);   // [0] length, [1] error bits
+    CR_CUDA(ctx, cudaMemcpyAsync(hist_pin, s->d_hist, sizeof(unsigned long long) * kPinHist, cudaMemcpyDeviceToHost, st));
+    CR_CUDA(ctx, cudaMemcpyAsync(&tail[0], s->d_hist_n, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CR_CUDA(ctx, cudaMemcpyAsync(&tail[1], s->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     CR_CUDA(ctx, cudaStreamSynchronize(st));
     float ms = 0;
     cudaEventElapsedTime(&ms, s->ev0, s->ev1);
     s->stats.main_ms += ms;
+    if (first) v1_init_pass1_time(s);
+    const int n = (int)tail[0];
+    const unsigned bits = tail[1];
     if (n <= 0 || n > kHistCap) return fail(ctx, CR_ERR_INTERNAL, "pass loop ran %d passes", n);
-    std::vector<unsigned long long> h(n);
-    CR_CUDA(ctx, cudaMemcpy(h.data(), s->d_hist, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost));
+    std::vector<unsigned long long> h(hist_pin, hist_pin + std::min(n, kPinHist));
+    if (n > kPinHist) {
+        h.resize(n);
+        CR_CUDA(ctx, cudaMemcpy(h.data() + kPinHist, s->d_hist + kPinHist, sizeof(unsigned long long) * (n - kPinHist),
+                                cudaMemcpyDeviceToHost));
+    }
+    const int loop_passes = first ? n - 1 : n;
     int per_pass = s->cols + 1;  // prep kernels and the loop's pass end
     for (int col = 0; col < s->cols; ++col)
         per_pass += col % 2 == 0 ? cop_launches_k(0, s->k, s->d_h1 != nullptr) : (col < s->cols - 1 ? cop_launches(1) : 1);
-    s->stats.kernel_launches += (int64_t)per_pass * n;
+    s->stats.kernel_launches += (int64_t)per_pass * loop_passes + 1;   // and the loop's start
     if (bits & kErrRank) return fail(ctx, CR_ERR_INTERNAL, "successor rank out of range");
     if (bits & kErrSlot) {
         // the last pass overflowed its value slots: keep the passes before it, widen the slots
@@ -945,15 +990,8 @@ int cr_solver_run(cr_solver* s, uint64_t* pass_counts, int32_t cap, int32_t* pas
     if (!s) return CR_ERR_INVALID;
     if (s->initialized && !s->finished && s->rules == CR_RULES_V1 && !s->ctx->profiling && !s->small) {
         CR_CUDA(s->ctx, cudaSetDevice(s->ctx->device));
-        if (s->init_pending) {
-            uint64_t f;
-            int rc = cr_solver_pass(s, &f);   // the fused first pass
-            if (rc) return rc;
-        }
-        if (!s->finished) {
-            int rc = v1_run_on_device(s);
-            if (rc) return rc;
-        }
+        int rc = v1_run_on_device(s);   // with the fused first pass when it is still pending
+        if (rc) return rc;
     }
     for (int i = 0; i < 1 << 16 && !s->finished; ++i) {
         uint64_t f;

@@ -108,7 +108,22 @@ __global__ void k_pass_end(const unsigned long long* counters, unsigned long lon
     cudaGraphSetConditional(loop, (f != 0ull && *err == 0u && i + 1 < cap) ? 1u : 0u);
 }
 
+// Start of a device-side pass loop: when the first pass ran just before the loop (*idx = 1,
+// set by the host) record its count as the history's first entry; loop while the last pass
+// found something and no error bit is set.
+__global__ void k_loop_start(const unsigned long long* counters, unsigned long long* hist, const int* idx,
+                             const unsigned* err, cudaGraphConditionalHandle loop) {
+    const unsigned long long f = counters[0];
+    if (*idx == 1) hist[0] = f;
+    cudaGraphSetConditional(loop, (f != 0ull && *err == 0u) ? 1u : 0u);
+}
+
 // ---------------------------------------------------------------- host-side launchers ---
+
+void launch_loop_start(const unsigned long long* counters, unsigned long long* hist, const int* idx,
+                       const unsigned* err, cudaGraphConditionalHandle loop, cudaStream_t st) {
+    k_loop_start<<<1, 1, 0, st>>>(counters, hist, idx, err, loop);
+}
 
 void launch_pass_end(const unsigned long long* counters, unsigned long long* hist, int* idx, int cap,
                      const unsigned* err, cudaGraphConditionalHandle loop, cudaStream_t st) {

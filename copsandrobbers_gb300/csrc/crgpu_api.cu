@@ -187,11 +187,20 @@ int cr_context_create(int32_t device, void* stream, cr_context** out) {
 int cr_context_destroy(cr_context* ctx) {
     if (!ctx) return CR_OK;
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    cudaSetDevice(ctx->device);
+    ctx->cache.clear();
     delete ctx;
     return CR_OK;
 }
 
 const char* cr_context_last_error(const cr_context* ctx) { return ctx ? ctx->err.c_str() : ""; }
+
+int cr_context_set_cache_limit(cr_context* ctx, uint64_t bytes) {
+    if (!ctx) return CR_ERR_INVALID;
+    CR_CUDA(ctx, cudaSetDevice(ctx->device));
+    ctx->cache.set_limit(bytes);
+    return CR_OK;
+}
 
 int cr_context_set_profiling(cr_context* ctx, int32_t on) {
     if (!ctx) return CR_ERR_INVALID;
@@ -289,8 +298,7 @@ static void free_v1(cr_solver* s) {
                     s->d_heads, s->d_trans, s->d_cand, s->d_cbits, s->d_list, s->d_clist, s->d_sync,
                     s->d_rrp, s->d_rcol, s->d_nbr, s->d_iso, s->d_rhop, s->d_cover,
                     s->d_crp, s->d_ccol, s->d_ciso, s->d_h1};
-    for (void* q : ptrs)
-        if (q) cudaFree(q);
+    for (void* q : ptrs) s->ctx->cache.put(q);   // the context keeps large blocks for reuse
     s->d_rp = nullptr; s->d_col = nullptr; s->d_binom = nullptr; s->d_configs = nullptr;
     s->d_hop = nullptr; s->d_table = nullptr; s->d_marked = nullptr; s->d_front = nullptr;
     s->d_fflag = nullptr; s->d_meta = nullptr; s->d_counters = nullptr; s->d_err = nullptr;
@@ -373,19 +381,19 @@ static std::vector<uint32_t> hop_masks(const cr_solver* s) {
 static int alloc_v1(cr_solver* s) {
     cr_context* ctx = s->ctx;
     const size_t C = s->C;
-    CR_CUDA(ctx, cudaMalloc(&s->d_table, C * s->n * s->cols));
-    CR_CUDA(ctx, cudaMalloc(&s->d_marked, (size_t)s->cols * C * s->rwp * 4));
-    CR_CUDA(ctx, cudaMalloc(&s->d_front, (size_t)s->cols * C * s->S * s->rwp * 4));
-    CR_CUDA(ctx, cudaMalloc(&s->d_fflag, (size_t)s->cols * C));
+    CR_CUDA(ctx, ctx->cache.get((void**)&s->d_table, C * s->n * s->cols));
+    CR_CUDA(ctx, ctx->cache.get((void**)&s->d_marked, (size_t)s->cols * C * s->rwp * 4));
+    CR_CUDA(ctx, ctx->cache.get((void**)&s->d_front, (size_t)s->cols * C * s->S * s->rwp * 4));
+    CR_CUDA(ctx, ctx->cache.get((void**)&s->d_fflag, (size_t)s->cols * C));
     CR_CUDA(ctx, cudaMalloc(&s->d_meta, sizeof(ColMeta) * s->cols));
-    CR_CUDA(ctx, cudaMalloc(&s->d_cand, C * s->S * s->rwp * 4));
-    CR_CUDA(ctx, cudaMalloc(&s->d_cbits, cand_bits_bytes(C)));
-    CR_CUDA(ctx, cudaMalloc(&s->d_list, (size_t)s->cols * C * 4));
-    CR_CUDA(ctx, cudaMalloc(&s->d_clist, C * 4));
+    CR_CUDA(ctx, ctx->cache.get((void**)&s->d_cand, C * s->S * s->rwp * 4));
+    CR_CUDA(ctx, ctx->cache.get((void**)&s->d_cbits, cand_bits_bytes(C)));
+    CR_CUDA(ctx, ctx->cache.get((void**)&s->d_list, (size_t)s->cols * C * 4));
+    CR_CUDA(ctx, ctx->cache.get((void**)&s->d_clist, C * 4));
     CR_CUDA(ctx, cudaMalloc(&s->d_sync, 2 * sizeof(unsigned)));
     CR_CUDA(ctx, cudaMemsetAsync(s->d_cand, 0, C * s->S * s->rwp * 4, ctx->stream));
     CR_CUDA(ctx, cudaMemsetAsync(s->d_cbits, 0, cand_bits_bytes(C), ctx->stream));
-    if (const uint64_t hb = h1_bytes(s->n, s->k, s->S, s->rwp)) CR_CUDA(ctx, cudaMalloc(&s->d_h1, hb));
+    if (const uint64_t hb = h1_bytes(s->n, s->k, s->S, s->rwp)) CR_CUDA(ctx, ctx->cache.get((void**)&s->d_h1, hb));
     CR_CUDA(ctx, cudaMalloc(&s->d_hop, (size_t)s->n * s->rwp * 4));
     std::vector<uint32_t> hop = hop_masks(s);
     CR_CUDA(ctx, cudaMemcpyAsync(s->d_hop, hop.data(), hop.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
@@ -562,7 +570,7 @@ int cr_solver_create(cr_context* ctx, const cr_graph* g, int32_t k, int32_t p, i
     CR_TRY(cudaMalloc(&s->d_rp, s->h_rp.size() * 4));
     CR_TRY(cudaMalloc(&s->d_col, std::max<size_t>(s->h_col.size(), 1) * 2));
     CR_TRY(cudaMalloc(&s->d_binom, s->h_binom.size() * 4));
-    CR_TRY(cudaMalloc(&s->d_configs, s->C * k * 2));
+    CR_TRY(ctx->cache.get((void**)&s->d_configs, s->C * k * 2));
     CR_TRY(cudaMalloc(&s->d_counters, 4 * sizeof(unsigned long long)));
     CR_TRY(cudaMalloc(&s->d_err, sizeof(unsigned int)));
     CR_TRY(cudaMallocHost(&s->h_pinned, (4 + kPinHist + 1) * sizeof(unsigned long long)));
@@ -804,11 +812,11 @@ static int grow_slots_and_replay(cr_solver* s) {
     cr_context* ctx = s->ctx;
     if (s->S >= 8) return fail(ctx, CR_ERR_INTERNAL, "frontier value range exceeds 8 slots");
     std::vector<uint64_t> done = s->pass_counts;
-    cudaFree(s->d_front);
+    ctx->cache.put(s->d_front);
     s->d_front = nullptr;
-    cudaFree(s->d_cand);
+    ctx->cache.put(s->d_cand);
     s->d_cand = nullptr;
-    if (s->d_h1) cudaFree(s->d_h1);
+    ctx->cache.put(s->d_h1);
     s->d_h1 = nullptr;
     if (s->pass_graph) cudaGraphExecDestroy(s->pass_graph);
     s->pass_graph = nullptr;
@@ -817,11 +825,11 @@ static int grow_slots_and_replay(cr_solver* s) {
     s->S *= 2;
     if (!pull_supported(s->S, s->rwp))
         return fail(ctx, CR_ERR_LIMIT, "row too wide for %d value slots", s->S);
-    CR_CUDA(ctx, cudaMalloc(&s->d_front, (size_t)s->cols * s->C * s->S * s->rwp * 4));
-    CR_CUDA(ctx, cudaMalloc(&s->d_cand, (size_t)s->C * s->S * s->rwp * 4));
+    CR_CUDA(ctx, ctx->cache.get((void**)&s->d_front, (size_t)s->cols * s->C * s->S * s->rwp * 4));
+    CR_CUDA(ctx, ctx->cache.get((void**)&s->d_cand, (size_t)s->C * s->S * s->rwp * 4));
     CR_CUDA(ctx, cudaMemsetAsync(s->d_cand, 0, (size_t)s->C * s->S * s->rwp * 4, ctx->stream));
     CR_CUDA(ctx, cudaMemsetAsync(s->d_cbits, 0, cand_bits_bytes(s->C), ctx->stream));
-    if (const uint64_t hb = h1_bytes(s->n, s->k, s->S, s->rwp)) CR_CUDA(ctx, cudaMalloc(&s->d_h1, hb));
+    if (const uint64_t hb = h1_bytes(s->n, s->k, s->S, s->rwp)) CR_CUDA(ctx, ctx->cache.get((void**)&s->d_h1, hb));
     const int per_sm = max_cop_blocks_per_sm(s->k, s->rwp, s->S);
     s->grid_cop = (int)std::max<uint64_t>(1, std::min<uint64_t>((s->C + 7) / 8, (uint64_t)ctx->num_sms * per_sm));
     uint64_t caps;

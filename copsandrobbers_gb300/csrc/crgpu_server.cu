@@ -13,6 +13,7 @@
 // one solver per request so every result is produced by the same code path as cr_solve.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -56,6 +57,9 @@ struct Request {
     cr_request_result res{};
     cr_solver* solver = nullptr;  // resident table until released
     cr_context* owner = nullptr;  // the worker context the solver lives on
+    const void* table = nullptr;  // its device table (taken by the worker once the solve is done)
+    size_t table_bytes = 0;
+    int readers = 0;              // client read-backs in flight; release waits for them
     std::string err;
 };
 
@@ -63,7 +67,11 @@ struct Request {
 
 struct cr_server {
     int device = 0;
-    uint64_t budget = 0, in_use = 0, peak_in_use = 0;
+    // budget = what requests may hold; reserve = what the workers' contexts may keep of freed
+    // solver buffers for reuse (their block caches), set aside from the caller's budget
+    uint64_t budget = 0, reserve = 0, in_use = 0, peak_in_use = 0;
+    cudaStream_t copy_stream = nullptr;   // client read-backs, apart from the workers' streams
+    std::mutex copy_mu;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     std::deque<Request*> queue;
@@ -96,6 +104,9 @@ void run_request(cr_server* srv, cr_context* ctx, Request* r) {
     if (!rc) rc = cr_solver_verdict(s, &v);
     if (!rc) rc = cr_solver_digest(s, &digest);
     if (!rc) rc = cr_solver_sizes(s, &sz);
+    void* table = nullptr;
+    size_t table_bytes = 0;
+    if (!rc) rc = cr_solver_device_states(s, &table, &table_bytes);
     std::lock_guard<std::mutex> lock(srv->mu);
     r->t_done = Clock::now();
     srv->t_last_done = r->t_done;
@@ -113,6 +124,8 @@ void run_request(cr_server* srv, cr_context* ctx, Request* r) {
     } else {
         r->solver = s;
         r->owner = ctx;
+        r->table = table;
+        r->table_bytes = table_bytes;
         r->res.win = v.win;
         r->res.capture_plies = v.capture_plies;
         r->res.best_config = v.best_config;
@@ -182,11 +195,21 @@ int cr_server_create(int32_t device, uint64_t memory_budget, int32_t workers, cr
         cudaMemGetInfo(&free_b, &total_b);
         memory_budget = (uint64_t)(free_b * 0.8);
     }
-    srv->budget = memory_budget;
+    // each worker context keeps up to `keep` bytes of freed solver buffers, so that requests of
+    // a size it has seen allocate nothing; that memory is set aside from the budget
+    const uint64_t keep = std::min<uint64_t>(1ull << 30, memory_budget / (8 * (uint64_t)workers));
+    srv->reserve = keep * (uint64_t)workers;
+    srv->budget = memory_budget - srv->reserve;
+    if (cudaStreamCreateWithFlags(&srv->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete srv;
+        return CR_ERR_CUDA;
+    }
     for (int i = 0; i < workers; ++i) {
         cr_context* c = nullptr;
-        if (cr_context_create(device, nullptr, &c) != CR_OK) {
+        if (cr_context_create(device, nullptr, &c) != CR_OK || cr_context_set_cache_limit(c, keep) != CR_OK) {
+            if (c) cr_context_destroy(c);
             for (cr_context* q : srv->contexts) cr_context_destroy(q);
+            cudaStreamDestroy(srv->copy_stream);
             delete srv;
             return CR_ERR_CUDA;
         }
@@ -253,27 +276,53 @@ int cr_server_poll(cr_server* srv, uint64_t id, int32_t wait_ms, cr_request_resu
     return CR_OK;
 }
 
+// The copy runs on the server's own stream from the client's thread: it touches neither the
+// worker's stream (which may be solving the next request) nor its context's error text, and the
+// request cannot be released while it runs (release waits for its readers).
 int cr_server_read_states(cr_server* srv, uint64_t id, uint8_t* dst, size_t bytes) {
     if (!srv || !dst) return CR_ERR_INVALID;
-    cr_solver* s = nullptr;
+    Request* r = nullptr;
     {
         std::lock_guard<std::mutex> lock(srv->mu);
         auto it = srv->reqs.find(id);
-        if (it == srv->reqs.end() || it->second->state != State::Done || !it->second->solver)
+        if (it == srv->reqs.end() || it->second->state != State::Done || !it->second->table)
             return CR_ERR_STATE;
-        s = it->second->solver;
+        r = it->second.get();
+        if (bytes < r->table_bytes) {
+            srv->err = "states buffer smaller than the table";
+            return CR_ERR_INVALID;
+        }
+        r->readers++;
     }
-    return cr_solver_read_states(s, dst, bytes);
+    cudaError_t e;
+    {
+        std::lock_guard<std::mutex> copy(srv->copy_mu);
+        e = cudaSetDevice(srv->device);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dst, r->table, r->table_bytes, cudaMemcpyDeviceToHost, srv->copy_stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(srv->copy_stream);
+    }
+    std::lock_guard<std::mutex> lock(srv->mu);
+    r->readers--;
+    srv->cv_done.notify_all();
+    if (e != cudaSuccess) {
+        srv->err = std::string("table read-back failed: ") + cudaGetErrorString(e);
+        return CR_ERR_CUDA;
+    }
+    return CR_OK;
 }
 
 int cr_server_release(cr_server* srv, uint64_t id) {
     if (!srv) return CR_ERR_INVALID;
     std::unique_ptr<Request> r;
     {
-        std::lock_guard<std::mutex> lock(srv->mu);
+        std::unique_lock<std::mutex> lock(srv->mu);
         auto it = srv->reqs.find(id);
         if (it == srv->reqs.end()) return CR_ERR_INVALID;
         if (it->second->state == State::Queued || it->second->state == State::Running) return CR_ERR_STATE;
+        Request* q = it->second.get();
+        srv->cv_done.wait(lock, [q] { return q->readers == 0; });   // a read-back in flight finishes first
+        it = srv->reqs.find(id);
+        if (it == srv->reqs.end()) return CR_ERR_INVALID;   // released by another thread meanwhile
         r = std::move(it->second);
         srv->reqs.erase(it);
         if (r->state == State::Done) srv->in_use -= r->footprint;
@@ -293,7 +342,7 @@ int cr_server_stats(cr_server* srv, cr_server_report* out) {
     out->queued = srv->queue.size();
     out->running = srv->running;
     out->max_running = srv->max_running;
-    out->memory_budget = srv->budget;
+    out->memory_budget = srv->budget + srv->reserve;
     out->memory_in_use = srv->in_use;
     out->peak_memory_in_use = srv->peak_in_use;
     out->states_done = srv->states_done;
@@ -315,6 +364,7 @@ int cr_server_destroy(cr_server* srv) {
         if (kv.second->solver) cr_solver_destroy(kv.second->solver);
     srv->reqs.clear();
     for (cr_context* c : srv->contexts) cr_context_destroy(c);
+    if (srv->copy_stream) cudaStreamDestroy(srv->copy_stream);
     delete srv;
     return CR_OK;
 }

@@ -93,6 +93,7 @@ SIGNATURES = {
     "cr_context_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "cr_context_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "cr_context_set_profiling": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    "cr_context_set_cache_limit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
     "cr_solver_footprint": (ctypes.c_uint64, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
     "cr_graph_parse": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t, c_i32p, c_u32p, c_u16p,
                                       ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),

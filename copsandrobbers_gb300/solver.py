@@ -34,6 +34,10 @@ class Context:
     def set_profiling(self, on: bool) -> None:
         _check(self.ptr, N.lib().cr_context_set_profiling(self.ptr, int(on)))
 
+    def set_cache_limit(self, nbytes: int) -> None:
+        """Bytes of freed solver buffers this context keeps for reuse (0 = none)."""
+        _check(self.ptr, N.lib().cr_context_set_cache_limit(self.ptr, int(nbytes)))
+
     def close(self) -> None:
         if self.ptr:
             N.lib().cr_context_destroy(self.ptr)

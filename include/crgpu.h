@@ -105,6 +105,12 @@ const char* cr_context_last_error(const cr_context* ctx);
 uint64_t cr_solver_footprint(int32_t n, int32_t k, int32_t p, int32_t rules);
 /* 1 = time every cop-turn launch with CUDA events (fills cop_step_ms), 0 = off. */
 int cr_context_set_profiling(cr_context* ctx, int32_t on);
+/* Bytes of freed solver buffers (blocks of 1 MiB or more) the context keeps for the next solve
+ * on it instead of returning them to the driver (default 4 GiB; 0 = keep none and release the
+ * held ones now).  Repeated solves of similar size -- cr_solve in a loop, a solve server's
+ * worker -- then allocate nothing.  No counterpart in the reference (it allocates host memory
+ * per run, lib/src/Allocator.cpp). */
+int cr_context_set_cache_limit(cr_context* ctx, uint64_t bytes);
 
 /* ---- graph input (lib/src/Graph.cpp:15-79, lib/src/AdjacencyList.cpp:33-76) -------- */
 

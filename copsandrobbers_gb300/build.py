@@ -25,7 +25,7 @@ EXE = os.path.join(BIN, "k_cops_gpu")
 
 CU_SOURCES = ["crgpu_api.cu", "crgpu_v1.cu", "crgpu_v2.cu", "crgpu_tables.cu", "crgpu_batch.cu",
               "crgpu_noalloc.cu", "crgpu_server.cu"]
-HEADERS = ["crgpu_internal.cuh", "crgpu_v1_body.cuh", "crgpu_ctx.h", "crgpu_v2.h", "crgpu_batch.h",
+HEADERS = ["crgpu_internal.cuh", "crgpu_v1_body.cuh", "crgpu_ctx.h", "crgpu_v2.h",
            os.path.join("..", "..", "include", "crgpu.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -47,6 +47,9 @@ def _stale(target: str, deps: list[str]) -> bool:
 def _compile(src: str) -> str:
     obj = os.path.join(OBJ, os.path.splitext(src)[0] + ".o")
     deps = [os.path.join(CSRC, src)] + [os.path.join(CSRC, h) for h in HEADERS]
+    missing = [d for d in deps if not os.path.exists(d)]
+    if missing:
+        raise RuntimeError(f"build dependencies missing: {missing}")
     if _stale(obj, deps):
         cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                "-I", os.path.join(ROOT, "include"), "-c", os.path.join(CSRC, src), "-o", obj]

@@ -14,7 +14,10 @@
 //     exits;
 //   * the first call on a device looks the array's device address up with
 //     cudaGetSymbolAddress (once per device, with that device current); make that first call
-//     before any stream capture;
+//     before any stream capture.  The address is kept for the process's life, so a
+//     cudaDeviceReset (which destroys the context the address belongs to) makes it stale;
+//   * it runs the general forms (unfused initializeCaptures, the tuple-gathering cop turn):
+//     the fused first pass and the separable turn need tables beyond the area;
 //   * all calls share the one array and leave the last call's contents in it: each call
 //     clears what must start at zero, and two calls whose work overlaps on the GPU (other
 //     streams, other host threads) race and corrupt each other;

@@ -302,7 +302,12 @@ int cr_server_destroy(cr_server* srv);
  *     n=128 with k=3 at p=1; larger solves return CR_ERR_LIMIT with the bytes needed in err.
  *   - Every GPU that loads the library holds the 64 MiB until the process exits.
  *   - The first call on a device looks up the array's device address (once per device);
- *     make it before any stream capture on that device.
+ *     make it before any stream capture on that device.  The address is kept for the life of
+ *     the process: after a cudaDeviceReset (or anything else that destroys the device's
+ *     primary context) it is stale, so do not call this entry point again in that process.
+ *   - It runs the general forms only -- initializeCaptures unfused from pass 1 and the
+ *     tuple-gathering cop turn -- because the fused first pass's tables and the separable
+ *     turn's pair rows need memory beyond the area; it is slower than cr_solve.
  *   - All calls share the array and leave their contents in it; each call clears what must
  *     start at zero.  Calls whose GPU work overlaps (other streams or host threads) race.
  * stream: cudaStream_t or NULL.  pass_counts[0 .. *passes) receive the per-pass counts;

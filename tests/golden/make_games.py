@@ -50,7 +50,7 @@ def extractor_file(sol, graph, path):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("CR_REFERENCE_ROOT", "/root/reference")
     spec = importlib.util.spec_from_file_location("pge", os.path.join(ref, "util", "perfect_game_extractor.py"))
     pge = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(pge)

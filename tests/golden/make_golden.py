@@ -7,7 +7,8 @@ wrote: pass counts, base captures, verdict, start positions, capture time, and S
 digests of every section of the table file it saved.
 
 The matrices used are copied into tests/golden/matrices/ so the fixtures travel without the
-reference tree.  Re-run with:  python tests/golden/make_golden.py  (needs /root/reference).
+reference tree.  Re-run with:  python tests/golden/make_golden.py  (needs the reference tree, at
+CR_REFERENCE_ROOT or /root/reference).
 """
 from __future__ import annotations
 
@@ -25,7 +26,8 @@ sys.path.insert(0, ROOT)
 from oracle import oracle as O  # noqa: E402
 from copsandrobbers_gb300 import graphs as G  # noqa: E402
 
-REF_MATRICES = "/root/reference/assets/matrices"
+REF_ROOT = os.environ.get("CR_REFERENCE_ROOT", "/root/reference")
+REF_MATRICES = os.path.join(REF_ROOT, "assets", "matrices")
 OUT_MATRICES = os.path.join(HERE, "matrices")
 CASES = os.path.join(HERE, "cases.json")
 

@@ -50,8 +50,11 @@ def test_oracle_stay_rules_match_legacy_solver_live(tmp_path, i):
     path = tmp_path / "g.txt"
     G.save_matrix(g, path)
     out = subprocess.run([LEGACY, str(path), str(k)], capture_output=True, text=True, timeout=300).stdout
-    result = re.search(r"RESULT: (WIN|LOSS)", out).group(1)
+    m = re.search(r"RESULT: (WIN|LOSS)", out)
+    assert m is not None, f"legacy solver printed no result:\n{out[-500:]}"
+    result = m.group(1)
     pos = re.search(r"Optimal Cop Start Positions: \(([^)]*)\)", out)
+    assert result == "LOSS" or pos is not None, f"legacy solver printed no start positions:\n{out[-500:]}"
     sol = O.solve_v1(g, k, 1, cop_stay=True, robber_stay=True)
     cid = first_universal_win(sol)
     assert (cid >= 0) == (result == "WIN")

@@ -164,11 +164,13 @@ def cpu_baseline(graph, k: int, p: int, passes: int, budget_s: float = 20.0) -> 
                       f"({swept} states, {t_total:.1f} s), scaled by the solve's {passes} passes"}
 
 
-def batched_workload(ctx, count: int = 4096, plain_sample: int = 128) -> dict:
+def batched_workload(ctx, count: int = 4096) -> dict:
     """Cop numbers of `count` seeded connected G(n, p) graphs, n ~ U[16, 128], mean degree
     ~ U[3, 6], k = 1, 2, 3 in order: one persistent launch (cr_batch_solve) against the plain
-    form -- one solve per (graph, k) through the public API -- timed on an evenly spaced sample
-    of the graphs and checked table by table (digests and pass-count hashes)."""
+    form -- one solve per (graph, k) through the public API on the same context, whose block
+    cache reuses the state store from solve to solve -- over every (graph, k) the batch solved.
+    The plain form's timed loop keeps each solve's pass counts; every table digest is taken in
+    a second, untimed loop and compared with the batch's, as is every pass-count hash."""
     import numpy as np
 
     from copsandrobbers_gb300 import graphs as G
@@ -181,27 +183,36 @@ def batched_workload(ctx, count: int = 4096, plain_sample: int = 128) -> dict:
     batch_solve(ctx, graphs, 3, 1, 0)  # warm-up (the autotuner calibrates on this batch)
     out = batch_solve(ctx, graphs, 3, 1, 0)
     batched = out.stats.states / (out.stats.ms / 1e3)
-    sample = list(range(0, count, max(1, count // plain_sample)))
+    jobs = [(gi, k) for gi in range(count) for k in range(1, 4) if out.results[gi][k - 1]["solved"]]
+    for gi, k in jobs[:32]:   # warm-up of the plain form (fills the context's block cache)
+        with Solver(ctx, graphs[gi], k, 1) as s:
+            s.init()
+            s.run()
+    hashes = []
     t0 = time.perf_counter()
-    states, mismatch = 0, 0
-    for gi in sample:
-        for k in range(1, 4):
-            r = out.results[gi][k - 1]
-            if not r["solved"]:
-                break
-            with Solver(ctx, graphs[gi], k, 1) as s:
-                s.init()
-                cnt = s.run()
-                dg = solver_digest(s)
-            states += int(r["states"])
-            mismatch += int(dg != r["digest"] or N.pass_hash(cnt) != r["pass_hash"])
-    plain = states / (time.perf_counter() - t0)
+    for gi, k in jobs:
+        with Solver(ctx, graphs[gi], k, 1) as s:
+            s.init()
+            hashes.append(N.pass_hash(s.run()))
+    plain_s = time.perf_counter() - t0
+    states = sum(int(out.results[gi][k - 1]["states"]) for gi, k in jobs)
+    mismatch = 0
+    for (gi, k), ph in zip(jobs, hashes):
+        r = out.results[gi][k - 1]
+        with Solver(ctx, graphs[gi], k, 1) as s:
+            s.init()
+            s.run()
+            dg = solver_digest(s)
+        mismatch += int(dg != r["digest"] or ph != r["pass_hash"])
+    plain = states / plain_s
     return {"workload": f"{count} connected G(n,p), n~U[16,128], mean degree~U[3,6], k=1..3 until WIN",
             "batched_states_per_s": batched, "plain_states_per_s": plain,
-            "batched_over_plain": batched / plain, "batched_ms": out.stats.ms,
+            "batched_over_plain": batched / plain, "batched_ms": out.stats.ms, "plain_ms": plain_s * 1e3,
             "states": int(out.stats.states), "ctas": int(out.stats.ctas), "threads": int(out.stats.threads),
             "busy_frac": float(out.stats.busy_frac), "tail_ms": float(out.stats.tail_ms),
-            "plain_sample_graphs": len(sample), "table_mismatches": mismatch,
+            "plain_sample_graphs": count, "plain_solves": len(jobs), "table_mismatches": mismatch,
+            "plain_form": "one Solver per (graph, k): create, initializeCaptures, mainLoop, destroy; "
+                          "store blocks reused through the context's cache; digests outside the timed loop",
             "cop_number_histogram": [int(x) for x in np.bincount(out.cop_numbers, minlength=4)]}
 
 
@@ -231,8 +242,8 @@ def limited_visibility_workload(ctx) -> dict:
 def serving_workload(count: int, rate: float, workers: int = 16) -> dict:
     """A seeded Poisson stream of solve requests through the solve server (cr_server_*):
     4-regular / G(n, 4/(n-1)) / Delaunay-thinned graphs, n log-uniform in [20, 400], k in
-    {1, 2, 3}, 10% with visibility period p in [2, 4]; admission by device footprint, tables
-    resident until the client releases them."""
+    {1, 2, 3}, 10% with visibility period p in [2, 4] (half of those under the v2 rules, k <= 2);
+    admission by device footprint, tables resident until the client releases them."""
     from copsandrobbers_gb300.serving import Server, request_stream, run_stream
 
     t0 = time.perf_counter()
@@ -245,7 +256,7 @@ def serving_workload(count: int, rate: float, workers: int = 16) -> dict:
     lat_q = sorted(float(r["queue_ms"]) for r in out["results"])
     return {"workload": f"{count} Poisson arrivals at {rate:g} requests/s (seed 12): 4-regular / "
                         "G(n,p) mean degree 4 / Delaunay-thinned, n log-uniform in [20,400], k in {1,2,3}, "
-                        "10% with p in [2,4]",
+                        "10% with p in [2,4] (half of them v2 rules, k <= 2)",
             "rate_per_s": rate, "requests": count, "workers": workers, "wall_s": out["wall_s"],
             "p50_ms": out["p50_ms"], "p99_ms": out["p99_ms"], "mean_ms": out["mean_ms"],
             "queue_p50_ms": lat_q[len(lat_q) // 2] if lat_q else None,
@@ -457,7 +468,7 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--headline-only", action="store_true",
                     help="skip the batched, limited-visibility and serving workloads")
-    ap.add_argument("--serving-requests", type=int, default=2000)
+    ap.add_argument("--serving-requests", type=int, default=20000)
     ap.add_argument("--serving-rate", type=float, default=45.0, help="requests per second")
     args = ap.parse_args()
     if args.impl == "reference":

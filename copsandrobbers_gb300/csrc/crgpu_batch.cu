@@ -518,7 +518,7 @@ int launch_batch(cr_context* ctx, const BatchInputs& in, const std::vector<int32
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     void (*kern)(BatchDev) = shape.threads > 512 ? k_batch<true, 1024> : k_batch<true, 512>;
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    raise_smem_limit((const void*)kern, sm);
     cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
         kern<<<nblocks, shape.threads, sm, st>>>(b);

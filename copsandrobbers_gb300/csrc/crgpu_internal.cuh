@@ -16,6 +16,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <map>
+#include <mutex>
+
 namespace crgpu {
 
 constexpr int kMaxRound = 127;      // MAX_ROUND_COUNT, k_cops_visibility.cpp:26
@@ -110,6 +113,22 @@ struct V1Dev {
 };
 
 __host__ __device__ inline int round_words(int rw) { return rw <= 2 ? rw : (rw + 3) & ~3; }
+
+// Raises a kernel's dynamic shared-memory limit to at least `bytes` and never lowers it.  The
+// attribute belongs to the process, not to a stream or a solver: setting it to each launch's own
+// size would let a smaller solve on another host thread shrink it under a larger one's launch,
+// which then fails (or, for a kernel whose output is read without its own error check, leaves
+// stale data).
+inline cudaError_t raise_smem_limit(const void* kernel, size_t bytes) {
+    static std::mutex mu;
+    static std::map<const void*, size_t> set;
+    std::lock_guard<std::mutex> lock(mu);
+    size_t& cur = set[kernel];
+    if (bytes <= cur) return cudaSuccess;
+    const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) cur = bytes;
+    return e;
+}
 
 // Valid robber bits of word w of a row (the tail word of a row is partial).
 __device__ __forceinline__ uint32_t valid_mask(int n, int w) {

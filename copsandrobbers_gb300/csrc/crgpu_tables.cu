@@ -179,7 +179,7 @@ void launch_trans(int k, const uint16_t* configs, uint32_t C, int n, const uint3
     const size_t sm = (size_t)warps * cap * sizeof(uint32_t);
 #define CR_TRANS(KK)                                                                        \
     {                                                                                       \
-        cudaFuncSetAttribute(k_trans<KK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm); \
+        raise_smem_limit((const void*)k_trans<KK>, sm); \
         k_trans<KK><<<grid, warps * 32, sm, st>>>(configs, C, n, rp, adj, B, cap, counts, heads, data, err); \
     }
     switch (k) {

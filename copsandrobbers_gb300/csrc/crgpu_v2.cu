@@ -792,13 +792,13 @@ int v2_init(V2Solver* s, uint64_t* caps, cr_solve_stats* stats, std::string* err
 template <int K, int W>
 static int launch_v2_val1(V2Solver* s, V2Dev d, uint64_t lo, uint64_t hi, int grid_pairs, size_t sm) {
     cudaStream_t st = s->st;
-    cudaFuncSetAttribute(k_v2_val1<K, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    raise_smem_limit((const void*)k_v2_val1<K, W>, sm);
     d.node_lo = lo;
     d.node_hi = hi;
     int launches = 0;
     if (d.hkey) {
-        cudaFuncSetAttribute(k_v2_hinsert<K, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        cudaFuncSetAttribute(k_v2_heval<K, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        raise_smem_limit((const void*)k_v2_hinsert<K, W>, sm);
+        raise_smem_limit((const void*)k_v2_heval<K, W>, sm);
         cudaMemsetAsync(d.hkey, 0, d.hcap * sizeof(unsigned long long), st);
         k_v2_hinsert<K, W><<<grid_pairs, 256, sm, st>>>(d);
         const int grid_h = (int)std::max<uint64_t>(1, std::min<uint64_t>((d.hcap + 255) / 256, (uint64_t)s->num_sms * 8));
@@ -817,7 +817,7 @@ static int launch_v2_kernels(V2Solver* s, const V2Dev& d, int grid_pairs, int gr
     const uint64_t chunk = d.hkey ? std::max<uint64_t>(1, s->chunk_nodes) : nodes;
     for (uint64_t lo = 0; lo < nodes; lo += chunk)
         launches += launch_v2_val1<K, W>(s, d, lo, std::min(nodes, lo + chunk), grid_pairs, sm);
-    cudaFuncSetAttribute(k_v2_root<K, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    raise_smem_limit((const void*)k_v2_root<K, W>, sm);
     k_v2_root<K, W><<<grid_cfg, 256, sm, s->st>>>(d);
     return launches + 1;
 }

@@ -4,8 +4,10 @@
 footprint as memory and workers free up, solved concurrently on per-worker streams, and their
 tables stay resident until released.  ``request_stream`` draws the serving workload: a mix of
 4-regular, Erdos-Renyi (mean degree 4) and Delaunay-thinned graphs with n log-uniform in
-[20, 400], k uniform in {1, 2, 3}, 10% of requests with visibility period p in [2, 4] (v1
-rules, 2p columns), and Poisson arrival times at a given rate.  ``run_stream`` replays it.
+[20, 400], k uniform in {1, 2, 3}, 10% of requests with visibility period p in [2, 4] -- half
+of those under the v1 rules (2p columns), half under the v2 macro-turn rules with k <= 2 (the
+reference's v2 search at k = 3 runs for minutes on small graphs) -- and Poisson arrival times at
+a given rate.  ``run_stream`` replays it.
 """
 from __future__ import annotations
 
@@ -84,6 +86,7 @@ class Request:
     p: int
     kind: str
     arrival_s: float
+    rules: int = N.CR_RULES_V1
 
 
 def _delaunay_fast(n: int, seed: int, mean_degree: float = 4.5) -> G.Graph:
@@ -148,9 +151,13 @@ def _er_connected_fast(n: int, mean_degree: float, seed: int) -> G.Graph:
     return G.Graph(adj)
 
 
-def request_stream(count: int, rate_per_s: float, seed: int = 7, n_lo: int = 20, n_hi: int = 400) -> list:
-    """The seeded serving workload (graphs, k, p and Poisson arrival times)."""
+def request_stream(count: int, rate_per_s: float, seed: int = 7, n_lo: int = 20, n_hi: int = 400,
+                   p_share: float = 0.10, v2_share: float = 0.5) -> list:
+    """The seeded serving workload (graphs, k, p, rules and Poisson arrival times).  A share
+    p_share of the requests has a visibility period p in [2, 4]; v2_share of those use the v2
+    rules (drawn from a second seeded stream, so the rest of the workload is unchanged)."""
     rng = np.random.default_rng(seed)
+    vrng = np.random.default_rng(seed ^ 0x5EED)
     gaps = rng.exponential(1.0 / rate_per_s, size=count)
     arrivals = np.cumsum(gaps) - gaps[0]
     out = []
@@ -158,7 +165,11 @@ def request_stream(count: int, rate_per_s: float, seed: int = 7, n_lo: int = 20,
         n = int(round(np.exp(rng.uniform(np.log(n_lo), np.log(n_hi)))))
         kind = ("regular4", "er4", "delaunay")[int(rng.integers(0, 3))]
         k = int(rng.integers(1, 4))
-        p = int(rng.integers(2, 5)) if rng.random() < 0.10 else 1
+        p = int(rng.integers(2, 5)) if rng.random() < p_share else 1
+        rules = N.CR_RULES_V1
+        if p > 1 and vrng.random() < v2_share:
+            rules = N.CR_RULES_V2
+            k = min(k, 2)
         gs = G.sub_seed(seed, i) & 0xFFFFFFFF
         if kind == "regular4":
             g = G.regular4(n + (n % 2), gs)
@@ -166,7 +177,7 @@ def request_stream(count: int, rate_per_s: float, seed: int = 7, n_lo: int = 20,
             g = _er_connected_fast(n, 4.0, gs)
         else:
             g = _delaunay_fast(n, gs)
-        out.append(Request(g, k, p, kind, float(arrivals[i])))
+        out.append(Request(g, k, p, kind, float(arrivals[i]), rules))
     return out
 
 
@@ -181,7 +192,7 @@ def run_stream(server: Server, reqs: list, release: bool = True) -> dict:
             delay = r.arrival_s - (time.perf_counter() - t0)
             if delay > 0:
                 time.sleep(delay)
-            ids[i] = server.submit(r.graph, r.k, r.p)
+            ids[i] = server.submit(r.graph, r.k, r.p, r.rules)
 
     th = threading.Thread(target=submitter)
     th.start()
@@ -201,4 +212,5 @@ def run_stream(server: Server, reqs: list, release: bool = True) -> dict:
     states = sum(int(d["states"]) for d in done)
     return {"requests": len(reqs), "wall_s": wall, "p50_ms": float(np.percentile(lat, 50)),
             "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()),
-            "states": states, "states_per_s": states / wall, "results": done, "stats": server.stats()}
+            "states": states, "states_per_s": states / wall, "results": done, "ids": ids,
+            "stats": server.stats()}

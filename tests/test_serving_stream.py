@@ -4,6 +4,7 @@ with visibility period p in [2, 4], connected graphs, Poisson arrivals at the st
 import numpy as np
 
 from copsandrobbers_gb300 import graphs as G
+from copsandrobbers_gb300 import native as N
 from copsandrobbers_gb300.serving import request_stream
 
 
@@ -23,6 +24,10 @@ def test_stream_mix():
     ps = np.array([r.p for r in reqs])
     assert set(ps[ps > 1]) <= {2, 3, 4}
     assert 0.05 < np.mean(ps > 1) < 0.15
+    # about half the limited-visibility requests use the v2 rules, with k <= 2; p = 1 is v1
+    v2 = [r for r in reqs if r.rules == N.CR_RULES_V2]
+    assert all(r.p > 1 and r.k <= 2 for r in v2)
+    assert 0.25 < len(v2) / max(1, int((ps > 1).sum())) < 0.75
     ns = np.array([r.graph.n for r in reqs])
     assert ns.min() >= 20 and ns.max() <= 81          # 4-regular graphs round n up to even
     for r in reqs[:100]:

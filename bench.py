@@ -242,7 +242,8 @@ def limited_visibility_workload(ctx) -> dict:
 def serving_workload(count: int, rate: float, workers: int = 16) -> dict:
     """A seeded Poisson stream of solve requests through the solve server (cr_server_*):
     4-regular / G(n, 4/(n-1)) / Delaunay-thinned graphs, n log-uniform in [20, 400], k in
-    {1, 2, 3}, 10% with visibility period p in [2, 4] (half of those under the v2 rules, k <= 2);
+    {1, 2, 3}, 10% with visibility period p in [2, 4] (half of those under the v2 rules with
+    k <= 2, p <= 3, n <= 200);
     admission by device footprint, tables resident until the client releases them."""
     from copsandrobbers_gb300.serving import Server, request_stream, run_stream
 
@@ -256,7 +257,7 @@ def serving_workload(count: int, rate: float, workers: int = 16) -> dict:
     lat_q = sorted(float(r["queue_ms"]) for r in out["results"])
     return {"workload": f"{count} Poisson arrivals at {rate:g} requests/s (seed 12): 4-regular / "
                         "G(n,p) mean degree 4 / Delaunay-thinned, n log-uniform in [20,400], k in {1,2,3}, "
-                        "10% with p in [2,4] (half of them v2 rules, k <= 2)",
+                        "10% with p in [2,4] (half of them v2 rules with k <= 2, p <= 3, n <= 200)",
             "rate_per_s": rate, "requests": count, "workers": workers, "wall_s": out["wall_s"],
             "p50_ms": out["p50_ms"], "p99_ms": out["p99_ms"], "mean_ms": out["mean_ms"],
             "queue_p50_ms": lat_q[len(lat_q) // 2] if lat_q else None,

@@ -83,7 +83,7 @@ __host__ __device__ inline uint64_t binom_dev(int64_t n, int64_t k) {
 
 // Byte offsets of one (n, k, p) solve inside a slot.
 struct JobLayout {
-    size_t binom, configs, nbr, iso, hop, rhop, table, marked, front, h1, list, clist, fflag, cand,
+    size_t binom, configs, nbr, iso, hop, rhop, cover, table, marked, front, h1, list, clist, fflag, cand,
         cbits, sync, meta, counters, err, total;
 };
 
@@ -103,6 +103,8 @@ __host__ __device__ inline JobLayout job_layout(int n, int k, int p, int S) {
     L.iso = take((size_t)rwp * 4);
     L.hop = take((size_t)n * rwp * 4);
     L.rhop = take((size_t)n * rwp * 4);
+    // uncovered-slot masks of the fused first pass (p = 1), up to 4 bytes per mask
+    L.cover = take(p == 1 ? 2 * (size_t)n * ((n + 7) & ~7) * 4 : 0);
     L.table = take(C * (size_t)n * cols);
     L.marked = take((size_t)cols * C * rwp * 4);
     L.front = take((size_t)cols * C * S * rwp * 4);
@@ -146,6 +148,57 @@ __device__ void block_fill(unsigned char* p, unsigned char v, size_t bytes) {
     const size_t n16 = bytes / 16;
     for (size_t i = threadIdx.x; i < n16; i += blockDim.x) p16[i] = q;
     for (size_t i = n16 * 16 + threadIdx.x; i < bytes; i += blockDim.x) p[i] = v;
+}
+
+// The uncovered-slot masks of the fused first pass, as the stand-alone solver builds them on the
+// host (cover[c][r] bit j: r's j-th neighbour v is neither c nor a neighbour of c; cover[n+c][r]:
+// v is not c; a cop's own entry all ones, the rows of a cop without a move zero), W = 1, 2 or 4
+// bytes per mask by the largest degree.  Sets d.g.cover, cover_w and npad.
+__device__ void build_cover(V1Dev& d, uint8_t* cov, int maxdeg) {
+    const int n = d.g.n, rwp = d.g.rwp, npad = (n + 7) & ~7;
+    const int W = maxdeg <= 8 ? 1 : (maxdeg <= 16 ? 2 : 4);
+    const uint32_t ones = W == 4 ? 0xFFFFFFFFu : ((1u << (8 * W)) - 1u);
+    const size_t plane = (size_t)n * npad * W;
+    for (int t = threadIdx.x; t < n * npad; t += blockDim.x) {
+        const int c = t / npad, r = t - c * npad;
+        uint32_t m0 = 0, m1 = 0;
+        if (r < n) {
+            const uint32_t e0 = d.g.row_ptr[r], deg = d.g.row_ptr[r + 1] - e0;
+            for (uint32_t j = 0; j < deg; ++j) {
+                const int v = d.g.col[e0 + j];
+                if (v == c) continue;
+                m1 |= 1u << j;
+                if (!((d.g.nbr[(size_t)c * rwp + (v >> 5)] >> (v & 31)) & 1u)) m0 |= 1u << j;
+            }
+            if (r == c) m0 = ones;
+        }
+        if ((d.g.isolated[c >> 5] >> (c & 31)) & 1u) m0 = 0;
+        for (int q = 0; q < W; ++q) {
+            cov[(size_t)t * W + q] = (uint8_t)(m0 >> (8 * q));
+            cov[plane + (size_t)t * W + q] = (uint8_t)(m1 >> (8 * q));
+        }
+    }
+    d.g.cover = cov;
+    d.g.cover_w = W;
+    d.g.npad = npad;
+    __syncthreads();
+}
+
+// Column col's row list from its flag plane, by the whole block (after the fused first pass).
+__device__ void block_list_compact(const V1Dev& d, int col) {
+    const uint8_t* f = d.fflag + (size_t)col * d.C;
+    uint32_t* out = d.list + (size_t)col * d.C;
+    const int lane = threadIdx.x & 31;
+    for (uint32_t base = threadIdx.x & ~31u; base < d.C; base += blockDim.x) {
+        const uint32_t i = base + lane;
+        const bool set = i < d.C && f[i];
+        const unsigned b = __ballot_sync(0xFFFFFFFFu, set);
+        if (!b) continue;
+        int at = 0;
+        if (lane == 0) at = atomicAdd(&d.meta[col].len, __popc(b));
+        at = __shfl_sync(0xFFFFFFFFu, at, 0);
+        if (set) out[at + __popc(b & ((1u << lane) - 1u))] = i;
+    }
 }
 
 // One (graph, k) solve by the whole block.  Returns 1 on WIN.
@@ -201,11 +254,18 @@ __device__ int solve_job(const BatchDev& b, unsigned char* slot, int gi, int jr,
     uint32_t* hop = reinterpret_cast<uint32_t*>(slot + L.hop);
     uint16_t* configs = reinterpret_cast<uint16_t*>(slot + L.configs);
 
+    // initializeCaptures and pass 1 fused (as the stand-alone p = 1 solve does) when the
+    // uncovered-slot masks fit: the first pass then writes every table byte and both marked
+    // planes itself
+    const int maxdeg = b.maxdeg[gi];
+    const bool fused = P1 && maxdeg <= 32;
     // ---- buildAuxGraph: zeroed planes, rank table, neighbour masks, configurations
-    block_fill(slot + L.nbr, 0, L.table - L.nbr);
-    block_fill(slot + L.marked, 0, L.front - L.marked);
+    block_fill(slot + L.nbr, 0, L.cover - L.nbr);
+    if (!fused) {
+        block_fill(slot + L.marked, 0, L.front - L.marked);
+        block_fill(d.table, kUnmarked, C * (size_t)n * cols);
+    }
     block_fill(slot + L.fflag, 0, L.total - L.fflag);
-    block_fill(d.table, kUnmarked, C * (size_t)n * cols);
     const int np1 = n + 1;
     for (int t = threadIdx.x; t < K * np1; t += blockDim.x) {
         const int i = t / np1, x = t - i * np1;
@@ -262,21 +322,46 @@ __device__ int solve_job(const BatchDev& b, unsigned char* slot, int gi, int jr,
             for (int w = 0; w < rwp; ++w) hop[(size_t)r * rwp + w] = cur[w];
         }
     }
-    // ---- initializeCaptures
-    if (threadIdx.x == 0) {
-        for (int c = 0; c < cols; ++c) d.meta[c] = ColMeta{0, kEmptyLo, -1, 0, 0, 0, 0, 0};
-        d.meta[0] = ColMeta{0, 0, 0, 1, (int)C, 0, -1, 0};
-        d.meta[1] = ColMeta{0, 0, 0, 0, (int)C, 1, -1, 0};
-    }
-    __syncthreads();
-    init_body(d, K, 0, 1);
-    __syncthreads();
-    const uint64_t caps = *d.pass_new;
-    __syncthreads();
-    // ---- mainLoop
-    uint64_t phash = 0;
+    uint64_t caps = 0, phash = 0;
     int passes = 0;
-    for (;;) {
+    bool more = true;
+    if (fused) {
+        build_cover(d, slot + L.cover, maxdeg);
+        if (threadIdx.x == 0) {
+            for (int c = 0; c < cols; ++c) d.meta[c] = ColMeta{0, kEmptyLo, -1, 0, 0, 0, 0, 0};
+            d.meta[0] = ColMeta{0, 0, 0, 0, (int)C, 0, -1, 0};
+            d.meta[1] = ColMeta{1, kEmptyLo, -1, 0, 0, 0, 0, 0};
+        }
+        __syncthreads();
+        if (d.g.cover_w == 1) init_pass1_body<K, 1>(d, 0, 1);
+        else if (d.g.cover_w == 2) init_pass1_body<K, 2>(d, 0, 1);
+        else init_pass1_body<K, 4>(d, 0, 1);
+        __syncthreads();
+        block_list_compact(d, 1);
+        __syncthreads();
+        // every configuration's distinct cops: n times the multisets holding a given vertex
+        caps = (uint64_t)n * (binom_dev((int64_t)n + K - 1, K) - binom_dev((int64_t)n + K - 2, K));
+        const uint64_t found = *d.pass_new;
+        const unsigned bits = *d.err;
+        __syncthreads();
+        passes = 1;
+        phash = mix64(found ^ (1ull * 0xD1B54A32D192ED03ull));
+        more = found != 0 && !bits;
+    } else {
+        // ---- initializeCaptures
+        if (threadIdx.x == 0) {
+            for (int c = 0; c < cols; ++c) d.meta[c] = ColMeta{0, kEmptyLo, -1, 0, 0, 0, 0, 0};
+            d.meta[0] = ColMeta{0, 0, 0, 1, (int)C, 0, -1, 0};
+            d.meta[1] = ColMeta{0, 0, 0, 0, (int)C, 1, -1, 0};
+        }
+        __syncthreads();
+        init_body(d, K, 0, 1);
+        __syncthreads();
+        caps = *d.pass_new;
+        __syncthreads();
+    }
+    // ---- mainLoop
+    while (more) {
         for (int col = 0; col < cols; ++col) {
             const int nx = (col + 1) % cols;
             prep_body(d, col, nx, 0, 1);

@@ -5,9 +5,10 @@ footprint as memory and workers free up, solved concurrently on per-worker strea
 tables stay resident until released.  ``request_stream`` draws the serving workload: a mix of
 4-regular, Erdos-Renyi (mean degree 4) and Delaunay-thinned graphs with n log-uniform in
 [20, 400], k uniform in {1, 2, 3}, 10% of requests with visibility period p in [2, 4] -- half
-of those under the v1 rules (2p columns), half under the v2 macro-turn rules with k <= 2 (the
-reference's v2 search at k = 3 runs for minutes on small graphs) -- and Poisson arrival times at
-a given rate.  ``run_stream`` replays it.
+of those under the v1 rules (2p columns), half under the v2 macro-turn rules with k <= 2, p <= 3
+and n <= 200 (the v2 search grows steeply with k, p and n: at k = 2, p = 4 or n = 400 one solve
+takes seconds to minutes) -- and Poisson arrival times at a given rate.  ``run_stream``
+replays it.
 """
 from __future__ import annotations
 
@@ -168,8 +169,10 @@ def request_stream(count: int, rate_per_s: float, seed: int = 7, n_lo: int = 20,
         p = int(rng.integers(2, 5)) if rng.random() < p_share else 1
         rules = N.CR_RULES_V1
         if p > 1 and vrng.random() < v2_share:
+            # v2 requests stay where the macro-turn search takes at most about 0.1 s on this GPU
+            # (Delaunay n = 200, k = 2, p = 3); p = 4 or n = 400 at k = 2 run for seconds to minutes
             rules = N.CR_RULES_V2
-            k = min(k, 2)
+            k, p, n = min(k, 2), min(p, 3), min(n, 200)
         gs = G.sub_seed(seed, i) & 0xFFFFFFFF
         if kind == "regular4":
             g = G.regular4(n + (n % 2), gs)

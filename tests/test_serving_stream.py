@@ -26,7 +26,7 @@ def test_stream_mix():
     assert 0.05 < np.mean(ps > 1) < 0.15
     # about half the limited-visibility requests use the v2 rules, with k <= 2; p = 1 is v1
     v2 = [r for r in reqs if r.rules == N.CR_RULES_V2]
-    assert all(r.p > 1 and r.k <= 2 for r in v2)
+    assert all(1 < r.p <= 3 and r.k <= 2 and r.graph.n <= 201 for r in v2)
     assert 0.25 < len(v2) / max(1, int((ps > 1).sum())) < 0.75
     ns = np.array([r.graph.n for r in reqs])
     assert ns.min() >= 20 and ns.max() <= 81          # 4-regular graphs round n up to even

@@ -7,6 +7,11 @@
 #   k_cops_visibility     solvers/k_cops_visibility.cpp    (v1, 2p-column retrograde)
 #   k_cops_visibility_v2  solvers/k_cops_visibility_v2.cpp (v2, macro-turn search)
 #   k_cops_4              legacy/src/k_cops_4.cpp          (multithreaded, stay-allowed rules)
+#   k_cops_visibility_stayCR  solvers/k_cops_visibility.cpp with its two self-edge switches
+#                         (lines 63-64: SelfEdgeCop, SelfEdgeRobber) set to C, R (1 = TRUE):
+#                         the stay-allowed rule sets 10, 01 and 11.  The switches are flipped in
+#                         a temporary copy outside this repository; the reference tree is
+#                         untouched and no reference source is kept.
 #
 # The reference's own build (build.py) is not used.  `-include cstddef` is needed
 # because lib/include/Graph.h and AdjacencyList.h use size_t without its header
@@ -22,7 +27,7 @@ if [ ! -d "$REF/solvers" ]; then
 fi
 mkdir -p "$OUT"
 if [ -x "$OUT/k_cops_visibility" ] && [ -x "$OUT/k_cops_visibility_v2" ] && [ -x "$OUT/k_cops_4" ] \
-   && [ -z "${CR_REBUILD_REF:-}" ]; then
+   && [ -x "$OUT/k_cops_visibility_stay11" ] && [ -z "${CR_REBUILD_REF:-}" ]; then
     exit 0   # already built (set CR_REBUILD_REF=1 to force)
 fi
 CXX="${CXX:-g++}"
@@ -37,5 +42,18 @@ build_solver solvers/k_cops_visibility.cpp k_cops_visibility &
 build_solver solvers/k_cops_visibility_v2.cpp k_cops_visibility_v2 &
 "$CXX" "${FLAGS[@]}" -pthread "$REF/legacy/src/k_cops_4.cpp" "$REF/lib/src/Graph.cpp" \
     "$REF/lib/src/AdjacencyList.cpp" "$REF/lib/src/fileio.cpp" -o "$OUT/k_cops_4" &
+STAY_TMP="$(mktemp -d)"
+for rules in "TRUE FALSE 10" "FALSE TRUE 01" "TRUE TRUE 11"; do
+    set -- $rules
+    src="$STAY_TMP/k_cops_visibility_stay$3.cpp"
+    sed -e "s/SelfEdgeCop c_edge = SelfEdgeCop::FALSE;/SelfEdgeCop c_edge = SelfEdgeCop::$1;/" \
+        -e "s/SelfEdgeRobber r_edge = SelfEdgeRobber::FALSE;/SelfEdgeRobber r_edge = SelfEdgeRobber::$2;/" \
+        "$REF/solvers/k_cops_visibility.cpp" > "$src"
+    grep -q "SelfEdgeCop c_edge = SelfEdgeCop::$1;" "$src" && grep -q "SelfEdgeRobber r_edge = SelfEdgeRobber::$2;" "$src" \
+        || { echo "build_ref: the self-edge switches were not found" >&2; exit 1; }
+    "$CXX" "${FLAGS[@]}" "-DALGORITHM_INCLUDE=\"$src\"" "$REF/app/main.cpp" "${LIBSRC[@]}" \
+        -o "$OUT/k_cops_visibility_stay$3" &
+done
 wait
+rm -rf "$STAY_TMP"
 echo "build_ref: built $(ls "$OUT" | tr '\n' ' ')"

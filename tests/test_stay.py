@@ -60,3 +60,19 @@ def test_oracle_stay_rules_match_legacy_solver_live(tmp_path, i):
     assert (cid >= 0) == (result == "WIN")
     if cid >= 0:
         assert [int(x) for x in sol.configs[cid]] == [int(x) for x in pos.group(1).split(",")]
+
+
+STAY_TABLES = json.load(open(os.path.join(GOLDEN, "stay_tables.json")))["cases"]
+
+
+@pytest.mark.parametrize("case", [c for c in STAY_TABLES if not c.get("large")],
+                         ids=lambda c: f"{c['graph']}-k{c['k']}-p{c['p']}-stay{c['cop_stay']}{c['robber_stay']}")
+def test_oracle_stay_tables_match_reference(case):
+    """The oracle's stay-rule sweep reproduces the reference v1 solver built with its self-edge
+    switches flipped (tests/golden/stay_tables.json): pass counts, captures and the states."""
+    import hashlib
+    g = G.load_matrix(os.path.join(GOLDEN, case["matrix"]))
+    sol = O.solve_v1(g, case["k"], case["p"], cop_stay=bool(case["cop_stay"]), robber_stay=bool(case["robber_stay"]))
+    assert sol.pass_counts == case["pass_counts"]
+    assert sol.base_captures == case["base_captures"]
+    assert hashlib.sha256(sol.states.tobytes()).hexdigest() == case["sha_states"]

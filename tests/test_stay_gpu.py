@@ -1,14 +1,22 @@
 """Stay-allowed rules on the device (CR_COP_STAY / CR_ROBBER_STAY): tables, pass counts and
-verdicts bit-exact against the oracle for every combination of the two flags."""
+verdicts bit-exact against the reference v1 solver built with its self-edge switches flipped
+(tests/golden/stay_tables.json, including two larger solves that take the push, separable and
+fused first-pass forms), and against the oracle on random graphs for every flag combination."""
+import hashlib
+import json
+import os
+
 import numpy as np
 import pytest
 
 from copsandrobbers_gb300 import graphs as G
 from copsandrobbers_gb300 import native as N
 from copsandrobbers_gb300.solver import solve
+from conftest import GOLDEN
 from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
+STAY_TABLES = json.load(open(os.path.join(GOLDEN, "stay_tables.json")))["cases"]
 FLAGS = [(False, False), (True, False), (False, True), (True, True)]
 
 
@@ -32,3 +40,18 @@ def test_stay_rules_refused_for_v2(gpu_ctx):
     with pytest.raises(N.CrGpuError) as e:
         solve(gpu_ctx, G.regular4(10, 1), 2, 2, N.CR_RULES_V2 | N.CR_COP_STAY)
     assert e.value.code == 4
+
+
+@pytest.mark.parametrize("case", STAY_TABLES,
+                         ids=lambda c: f"{c['graph']}-k{c['k']}-p{c['p']}-stay{c['cop_stay']}{c['robber_stay']}")
+def test_stay_tables_match_reference(gpu_ctx, case):
+    g = G.load_matrix(os.path.join(GOLDEN, case["matrix"]))
+    rules = N.CR_RULES_V1 | (N.CR_COP_STAY if case["cop_stay"] else 0) | (N.CR_ROBBER_STAY if case["robber_stay"] else 0)
+    r = solve(gpu_ctx, g, case["k"], case["p"], rules)
+    assert r.pass_counts == case["pass_counts"]
+    assert r.base_captures == case["base_captures"]
+    assert hashlib.sha256(r.states.tobytes()).hexdigest() == case["sha_states"]
+    assert r.verdict.win == (case["result"] == "WIN")
+    if r.verdict.win:
+        assert ",".join(str(x) for x in r.verdict.positions) == case["positions"].replace(" ", "")
+        assert r.verdict.capture_plies == case["capture_plies"]

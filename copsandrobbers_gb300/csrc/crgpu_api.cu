@@ -1265,7 +1265,6 @@ int cr_solver_write_table_file(cr_solver* s, const char* path) {
 int cr_solver_load_table_file(cr_solver* s, const char* path) {
     if (!s || !path) return CR_ERR_INVALID;
     cr_context* ctx = s->ctx;
-    if (s->rules != CR_RULES_V1) return fail(ctx, CR_ERR_LIMIT, "table files load into v1 solvers");
     if (s->n > 256) return fail(ctx, CR_ERR_LIMIT, "the table file stores vertices as uint8 (n <= 256)");
     FILE* f = fopen(path, "rb");
     if (!f) return fail(ctx, CR_ERR_IO, "cannot open %s", path);
@@ -1306,9 +1305,15 @@ int cr_solver_load_table_file(cr_solver* s, const char* path) {
     s->n_trans = ntrans;
     CR_CUDA(ctx, cudaMemcpyAsync(s->d_heads, blob.data() + h[9], heads, cudaMemcpyHostToDevice, st));
     if (ntrans) CR_CUDA(ctx, cudaMemcpyAsync(s->d_trans, blob.data() + h[10], ntrans * 8, cudaMemcpyHostToDevice, st));
-    CR_CUDA(ctx, cudaMemcpyAsync(s->d_table, blob.data() + h[11], states, cudaMemcpyHostToDevice, st));
-    launch_marks_from_table(s->d_table, (uint32_t)s->C, s->n, s->cols, s->rwp, s->d_marked, ctx->num_sms * 8, st);
-    CR_CUDA(ctx, cudaGetLastError());
+    if (s->rules == CR_RULES_V2) {
+        // the single-plane store of the v2 solver (k_cops_visibility_v2.cpp:170-182 loads the
+        // same file layout with one column)
+        if (int rc2 = crgpu::v2_load_states(s->v2, blob.data() + h[11], &ctx->err)) return rc2;
+    } else {
+        CR_CUDA(ctx, cudaMemcpyAsync(s->d_table, blob.data() + h[11], states, cudaMemcpyHostToDevice, st));
+        launch_marks_from_table(s->d_table, (uint32_t)s->C, s->n, s->cols, s->rwp, s->d_marked, ctx->num_sms * 8, st);
+        CR_CUDA(ctx, cudaGetLastError());
+    }
     CR_CUDA(ctx, cudaStreamSynchronize(st));   // the host blob goes out of scope
     s->init_pending = false;
     s->initialized = true;

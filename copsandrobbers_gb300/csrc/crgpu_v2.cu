@@ -47,6 +47,8 @@
 
 namespace crgpu {
 
+void launch_marks_from_table(const uint8_t* table, uint32_t C, int n, int cols, int rwp, uint32_t* marked,
+                             int grid, cudaStream_t st);
 void launch_verdict_raw(const uint8_t* table, const uint32_t* m0, uint32_t C, int n, int rw,
                         int rwp, int cols, unsigned long long* best, int grid, cudaStream_t st);
 
@@ -894,6 +896,15 @@ int v2_pass(V2Solver* s, uint64_t* found, cr_solve_stats* stats, std::string* er
     cudaEventElapsedTime(&ms, s->e0, s->e1);
     stats->main_ms += ms;
     stats->kernel_launches += launches;
+    return CR_OK;
+}
+
+int v2_load_states(V2Solver* s, const uint8_t* states, std::string* err) {
+    cudaStream_t st = s->st;
+    V2_CUDA(cudaMemcpyAsync(s->table, states, (size_t)s->C * s->n, cudaMemcpyHostToDevice, st));
+    launch_marks_from_table(s->table, s->C, s->n, 1, s->rwp, s->marked, s->num_sms * 8, st);
+    V2_CUDA(cudaGetLastError());
+    V2_CUDA(cudaStreamSynchronize(st));   // the caller's host buffer goes out of scope
     return CR_OK;
 }
 

@@ -23,5 +23,8 @@ void v2_verdict(V2Solver* s, unsigned long long* best_key);
 const uint8_t* v2_table(const V2Solver* s);
 cr_v2_hash_stats v2_hash_stats(const V2Solver* s);
 int v2_set_hash_capacity(V2Solver* s, uint64_t slots, std::string* err);
+// A solved single-plane table (C * n bytes, host memory) loaded as the store: the table
+// uploaded and its marked plane rebuilt on the device.
+int v2_load_states(V2Solver* s, const uint8_t* states, std::string* err);
 
 }  // namespace crgpu

@@ -121,16 +121,16 @@ bool buildAuxGraph() {
     if (report(cr_solver_create(g_ctx, &g, g_k, g_p, CR_GPU_RULES, &g_solver), "Unable to generate aux graph"))
         return 1;
     // CacheManager::loadAuxGraph (CacheManager.h:78-141): a table file under the same key whose
-    // header matches (self-edge flags 0/0 in words 6-7) is a hit.  v1 reads it into the device
-    // store; for v2 the header check alone decides.  initializeCaptures resets every column
-    // either way, so a hit and a miss solve identically.
+    // header matches (self-edge flags 0/0 in words 6-7) is a hit, and it is read into the device
+    // store (the key, sizes, sections and configs are checked as the reference checks them; v1
+    // and v2 alike).  initializeCaptures resets every column either way, so a hit and a miss
+    // solve identically.
     bool hit = false;
     if (FILE* f = std::fopen(cache_path().c_str(), "rb")) {
         uint64_t h[12];
         hit = std::fread(h, 8, 12, f) == 12 && h[6] == 0 && h[7] == 0;
         std::fclose(f);
-        if (hit && CR_GPU_RULES == CR_RULES_V1)
-            hit = cr_solver_load_table_file(g_solver, cache_path().c_str()) == CR_OK;
+        if (hit) hit = cr_solver_load_table_file(g_solver, cache_path().c_str()) == CR_OK;
     }
     if (hit) {
         std::cout << "Loaded AuxGraph from cache!\n";

@@ -153,8 +153,9 @@ int cr_solver_read_transitions(cr_solver* s, uint64_t* heads, size_t heads_len,
 /* outputData (k_cops_visibility.cpp:356-373; CacheManager::saveAuxGraph, CacheManager.h:28-75):
  * write the whole table file (96-byte header, configs, heads, transitions, states). */
 int cr_solver_write_table_file(cr_solver* s, const char* path);
-/* CacheManager::loadAuxGraph (CacheManager.h:78-141) into the device store (v1 rules): a table
- * file whose header matches this solver (k, n, columns, configs, states, self-edge flags) is
+/* CacheManager::loadAuxGraph (CacheManager.h:78-141; the v2 solver's hit at
+ * k_cops_visibility_v2.cpp:170-182 reads the same layout with one column) into the device
+ * store, v1 or v2 rules: a table file whose header matches this solver (k, n, columns, configs, states, self-edge flags) is
  * read back; its states section becomes the table, its heads and transitions sections the
  * successor CSR, its configs section is checked against the solver's own, and the marked
  * planes are rebuilt from the table bytes.  The loaded table answers cr_solver_verdict, the

@@ -54,3 +54,25 @@ def test_v2_table_file_bytes(gpu_ctx, tmp_path):
             path = str(tmp_path / "t.bin")
             s.write_table_file(path)
         assert hashlib.sha256(open(path, "rb").read()).hexdigest() == case["sha_file"], case_id(case)
+
+
+def test_v2_table_file_round_trip(gpu_ctx, tmp_path):
+    """The v2 cache hit (k_cops_visibility_v2.cpp:170-182 -> CacheManager.h:78-141): a written
+    v2 table file loads back into a fresh v2 solver as a solved table (same bytes and verdict);
+    a file written for another solve is refused; initializeCaptures then resets the table."""
+    for case in [c for c in V2 if c["graph"] in ("peterson", "grid9", "dodecahedron", "planar8")][:8]:
+        g = G.load_matrix(matrix_path(case))
+        path = str(tmp_path / "t2.bin")
+        with Solver(gpu_ctx, g, case["k"], case["p"], N.CR_RULES_V2) as s:
+            s.init(); counts = s.run()
+            s.write_table_file(path)
+            st, v = s.states(), s.verdict()
+        with Solver(gpu_ctx, g, case["k"], case["p"], N.CR_RULES_V2) as t:
+            t.load_table_file(path)
+            assert np.array_equal(t.states(), st) and t.verdict() == v, case_id(case)
+            t.init(); assert t.run() == counts
+            assert np.array_equal(t.states(), st)
+        with Solver(gpu_ctx, g, case["k"] % 2 + 1, case["p"], N.CR_RULES_V2) as u:   # another k
+            with pytest.raises(N.CrGpuError) as e:
+                u.load_table_file(path)
+            assert e.value.code in (1, 7)

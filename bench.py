@@ -129,6 +129,18 @@ def measured_peak_hbm() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
+def solve_dram_bytes() -> float | None:
+    """Measured DRAM bytes of one solve step (ncu over every launch) from the committed summary."""
+    path = os.path.join(ROOT, "profiles", "large_solve_n256_launches.md")
+    try:
+        for line in open(path):
+            if line.startswith("solve_dram_bytes:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
 def traffic_per_launch() -> float | None:
     """DRAM bytes per k_init_pass1 launch from the committed ncu summary, if present."""
     path = os.path.join(ROOT, "profiles", "k_init_pass1_large_n256.md")
@@ -381,6 +393,18 @@ def run_gpu(args) -> None:
     resolved = 2 * int(solver.base_captures) + sum(solver.pass_counts)
     solve_bytes = passes * 3 * S / 8 + 2 * resolved + S
     solve_achieved = solve_bytes / (ms / args.steps / 1e3) / 1e9
+    # the whole step, twice: by DRAM bytes measured with ncu over every launch of one solve
+    # (profiles/large_solve_n256_launches.md), and by the byte model above, labelled as such
+    dram = solve_dram_bytes()
+    step_s = ms / args.steps / 1e3
+    solve_roofline = {"dram_bytes": dram, "dram_gbs": dram / step_s / 1e9 if dram else None,
+                      "dram_frac": dram / step_s / 1e9 / measured_peak_hbm()[0] if dram else None,
+                      "dram_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum over one solve's launches",
+                      "model_bytes": solve_bytes, "model_gbs": solve_achieved,
+                      "model_frac": solve_achieved / measured_peak_hbm()[0],
+                      "model": "per level 3S/8 of bit planes + 2 B depth per resolved state + 1 B counter per "
+                               "state (a store layout with counter arrays; not traffic of this solver)",
+                      "levels": passes, "resolved_states": resolved}
     solver.close()
 
     # e2e: the public one-call API from pinned host CSR to the pinned host table
@@ -446,9 +470,7 @@ def run_gpu(args) -> None:
                          "frac": achieved / peak if achieved else None, "traffic": traffic,
                          "kernel": "k_init_pass1 (initializeCaptures + pass 1, one launch per solve)",
                          "peak_source": peak_kind, "mean_launch_ms": k_ms, "alg_bytes_per_launch": k_bytes,
-                         "solve": {"alg_bytes": solve_bytes, "achieved": solve_achieved,
-                                   "frac": solve_achieved / peak, "levels": passes,
-                                   "resolved_states": resolved}},
+                         "solve": solve_roofline},
             "cpu_baseline": base,
             "clocks": clocks.summary(),
             "gpu_launches": launches_per_step * args.steps,

@@ -75,10 +75,10 @@ struct V2Solver {
     unsigned long long* counters = nullptr;
     unsigned int* err = nullptr;
     unsigned long long* h_pinned = nullptr;
-    // depth-2 cloud table (p >= 3): keys, clouds [hcap][rwp] and subtree values
+    // depth-2 cloud table (p >= 3): key words (key and subtree value, see cloud_key) and
+    // clouds [hcap][rwp]
     unsigned long long* hkey = nullptr;
     uint32_t* hmask = nullptr;
-    uint8_t* hval = nullptr;
     uint64_t hcap = 0;
     uint64_t chunk_nodes = 0;   // depth-1 nodes per table fill
     cr_v2_hash_stats hstats{};
@@ -102,12 +102,12 @@ struct V2Dev {
     unsigned long long* count;     // [0] marks found, [1] depth-2 child visits, [2] table entries
     unsigned long long* hkey;      // null = no cloud table (p < 3)
     uint32_t* hmask;
-    uint8_t* hval;
     uint64_t hcap;                 // power of two
     uint64_t node_lo, node_hi;     // depth-1 nodes (C1 * n + r) of this chunk
 };
 
 constexpr int kHashProbes = 64;   // linear-probe limit of an insert or a lookup
+
 
 template <int W>
 struct Mask {
@@ -327,8 +327,9 @@ __device__ int node2_min_p3(const V2Dev& d, const int (&c2)[K], const Mask<W>& V
     return best;
 }
 
-// Cloud-table key of depth-2 node (cid, V): the config's rank + 1 above a 32-bit fingerprint
-// of the cloud (never 0, which marks an empty slot).
+// Cloud-table key of depth-2 node (cid, V): the config's rank + 1 above a 24-bit fingerprint of
+// the cloud, above a zero byte where the node's subtree value goes once k_v2_heval has it (one
+// word per probe holds both; never 0, which marks an empty slot).
 template <int W>
 __device__ __forceinline__ unsigned long long cloud_key(uint32_t cid, const Mask<W>& V) {
     uint32_t h = 0x9E3779B9u;
@@ -339,7 +340,7 @@ __device__ __forceinline__ unsigned long long cloud_key(uint32_t cid, const Mask
     }
     h *= 0xC2B2AE35u;
     h ^= h >> 16;
-    return ((unsigned long long)(cid + 1u) << 32) | h;
+    return ((unsigned long long)(cid + 1u) << 32) | ((h & 0xFFFFFFu) << 8);
 }
 
 __device__ __forceinline__ uint64_t cloud_slot(unsigned long long key, uint64_t cap) {
@@ -349,6 +350,8 @@ __device__ __forceinline__ uint64_t cloud_slot(unsigned long long key, uint64_t 
     return (z ^ (z >> 31)) & (cap - 1);
 }
 
+// Insert (cid, V) unless its key is present; the thread that claims a slot writes the cloud.
+// Returns 1 when this call claimed a new slot.
 // Insert (cid, V) unless its key is present; the thread that claims a slot writes the cloud.
 // Returns 1 when this call claimed a new slot.
 template <int W>
@@ -378,13 +381,13 @@ __device__ __forceinline__ int cloud_lookup(const V2Dev& d, uint32_t cid, const 
     for (int probe = 0; probe < kHashProbes; ++probe) {
         const unsigned long long k = __ldg(&d.hkey[h]);
         if (k == 0ull) return -1;
-        if (k == key) {
+        if ((k & ~0xFFull) == key) {
             const uint32_t* m = d.hmask + h * d.rwp;
             bool same = true;
 #pragma unroll
             for (int j = 0; j < W; ++j)
                 if (j < d.rwp) same &= __ldg(&m[j]) == V.w[j];
-            return same ? (int)__ldg(&d.hval[h]) : -1;
+            return same ? (int)(k & 0xFFull) : -1;
         }
         h = (h + 1) & (d.hcap - 1);
     }
@@ -467,7 +470,7 @@ __global__ void __launch_bounds__(256) k_v2_heval(V2Dev d) {
 #pragma unroll
         for (int j = 0; j < W; ++j) V.w[j] = j < d.rwp ? d.hmask[h * d.rwp + j] : 0u;
         const int v = d.p == 3 ? node2_min_p3<W, K>(d, c2, V, snbr) : subtree_min<W, K>(d, c2, V, snbr, kV2None);
-        d.hval[h] = (uint8_t)min(v, kV2None);
+        d.hkey[h] = key | (unsigned long long)min(v, kV2None);   // the value in the key word's low byte
     }
 }
 
@@ -642,7 +645,7 @@ uint64_t v2_footprint(int n, int k, int p) {
     const int rwp = round_words((n + 31) / 32);
     const uint64_t hcap = v2_hash_capacity(c * (uint64_t)n, p);
     return c * n * 3 + c * (uint64_t)rwp * 4 + c * 3 + (uint64_t)n * rwp * 4 + c * (uint64_t)k * 2 +
-           hcap * (8 + 4 * (uint64_t)rwp + 1) + (1u << 16);
+           hcap * (8 + 4 * (uint64_t)rwp) + (1u << 16);
 }
 
 static int v2_w(int rwp) { return rwp <= 1 ? 1 : rwp <= 2 ? 2 : rwp <= 4 ? 4 : rwp <= 8 ? 8 : 16; }
@@ -653,7 +656,7 @@ static V2Dev v2_view(const V2Solver* s) {
     d.rp = s->rp; d.col = s->col; d.binom = s->binom; d.configs = s->configs;
     d.table = s->table; d.marked = s->marked; d.nbr = s->nbr;
     d.val1 = s->val1; d.newval = s->newval; d.dirty = s->dirty; d.count = s->counters;
-    d.hkey = s->hkey; d.hmask = s->hmask; d.hval = s->hval; d.hcap = s->hcap;
+    d.hkey = s->hkey; d.hmask = s->hmask; d.hcap = s->hcap;
     d.node_lo = 0;
     d.node_hi = (uint64_t)s->C * s->n;
     return d;
@@ -680,28 +683,25 @@ int v2_set_hash_capacity(V2Solver* s, uint64_t slots, std::string* err) {
         while (cap < slots) cap <<= 1;
     }
     V2_CUDA(cudaStreamSynchronize(s->st));
-    void* old[] = {s->hkey, s->hmask, s->hval};
+    void* old[] = {s->hkey, s->hmask};
     for (void* q : old)
         if (q) cudaFree(q);
     s->hkey = nullptr;
     s->hmask = nullptr;
-    s->hval = nullptr;
     s->hcap = 0;
     s->chunk_nodes = 0;
     s->hstats.capacity = 0;
     if (!cap) return CR_OK;
-    // all three arrays or none: a solver whose table could not be allocated keeps working
-    // without one (every depth-2 node evaluated where it is reached)
+    // a solver whose table could not be allocated keeps working without one (every depth-2
+    // node evaluated where it is reached)
     cudaError_t e = cudaMalloc(&s->hkey, cap * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMalloc(&s->hmask, cap * s->rwp * sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaMalloc(&s->hval, cap);
     if (e != cudaSuccess) {
-        void* got[] = {s->hkey, s->hmask, s->hval};
+        void* got[] = {s->hkey, s->hmask};
         for (void* q : got)
             if (q) cudaFree(q);
         s->hkey = nullptr;
         s->hmask = nullptr;
-        s->hval = nullptr;
         if (err) *err = std::string("v2 cloud table: ") + cudaGetErrorString(e);
         return e == cudaErrorMemoryAllocation ? CR_ERR_NOMEM : CR_ERR_CUDA;
     }
@@ -754,7 +754,7 @@ int v2_create(V2Solver** out, cudaStream_t st, int num_sms, int n, int k, int p,
 void v2_destroy(V2Solver* s) {
     if (!s) return;
     void* ptrs[] = {s->table, s->marked, s->nbr, s->val1, s->newval, s->changed, s->dirty, s->tmp, s->counters,
-                    s->hkey, s->hmask, s->hval};
+                    s->hkey, s->hmask};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     if (s->h_pinned) cudaFreeHost(s->h_pinned);

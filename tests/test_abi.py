@@ -51,8 +51,9 @@ def test_footprint_counts_pair_rows_and_cloud_table():
     table_128 = 357_760 * 128 * 2
     pair_rows_128 = 128 * 129 // 2 * 128 * 2 * 4 * 4
     assert footprint(128, 3) > table_128 + pair_rows_128
-    # v2 with p >= 3 holds the cloud table: 2^23 slots of 8 + 4 * rwp + 1 bytes at n = 199, k = 2
-    assert footprint(199, 2, 3, N.CR_RULES_V2) - footprint(199, 2, 2, N.CR_RULES_V2) == (1 << 23) * (8 + 4 * 8 + 1)
+    # v2 with p >= 3 holds the cloud table: 2^23 slots of an 8-byte key word (key and value) and
+    # a 4 * rwp-byte cloud at n = 199, k = 2
+    assert footprint(199, 2, 3, N.CR_RULES_V2) - footprint(199, 2, 2, N.CR_RULES_V2) == (1 << 23) * (8 + 4 * 8)
 
 
 def test_missing_library_fails_loudly(monkeypatch, tmp_path):

@@ -153,6 +153,18 @@ def traffic_per_launch() -> float | None:
     return None
 
 
+def reference_code_timings() -> dict | None:
+    """The reference's own solvers timed by oracle/time_reference.py where the reference tree is
+    (its sources do not ship with this repository, and its x86-64 builds do not run on the Arm
+    GPU host): a record with the machine it came from, not a measurement of this run."""
+    path = os.path.join(ROOT, "oracle", "reference_timings.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return None
+
+
 def cpu_baseline(graph, k: int, p: int, passes: int, budget_s: float = 20.0) -> dict:
     """The oracle's restatement of the reference sweep on all host cores over a bounded sample."""
     from oracle import oracle as O
@@ -173,7 +185,8 @@ def cpu_baseline(graph, k: int, p: int, passes: int, budget_s: float = 20.0) -> 
     rate = swept / t_total / passes
     return {"value": rate, "unit": METRIC, "cores": cores, "kind": "port",
             "sample": f"one v1 pass (all {2 * p} columns) over {done_cfg} of {C} configurations "
-                      f"({swept} states, {t_total:.1f} s), scaled by the solve's {passes} passes"}
+                      f"({swept} states, {t_total:.1f} s), scaled by the solve's {passes} passes",
+            "reference_code": reference_code_timings()}
 
 
 def batched_workload(ctx, count: int = 4096) -> dict:
@@ -291,7 +304,10 @@ def run_reference(args) -> None:
     cores = os.cpu_count() or 1
     C = samp.count
     slice_cfg = max(1, C // 64)
-    passes = 5  # the pass count of this solve (the GPU arm and the oracle both find 5)
+    # the solve's pass count, from the oracle's full solve of this graph (tests/golden/large.json;
+    # the GPU arm finds the same): one pass over a slice of the configurations is timed per step
+    with open(os.path.join(ROOT, "tests", "golden", "large.json")) as f:
+        passes = len(json.load(f)["n256"]["pass_counts"])
 
     def step(i):
         c0 = (i * slice_cfg) % C
@@ -315,7 +331,8 @@ def run_reference(args) -> None:
         "vs_baseline": None, "dtype": "u8", "data": "synthetic (seeded generator)", "config": LARGE,
         "cpu_baseline": {"value": value, "unit": "states/s", "cores": cores, "kind": "port",
                          "sample": f"per step one v1 pass over {slice_cfg} of {C} configurations, "
-                                   f"scaled by the solve's {passes} passes"},
+                                   f"scaled by the solve's {passes} passes",
+                         "reference_code": reference_code_timings()},
         "e2e": {"value": value, "unit": "states/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

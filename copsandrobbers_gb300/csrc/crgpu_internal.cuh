@@ -44,6 +44,9 @@ struct ColMeta {
     int seed;    // 1 = the frontier is exactly the capture seeds (r on a cop, value 0)
     int len;     // rows in the column's list; -1 = every configuration (the list is implicit)
     int clean;   // 1 = the frontier's consumer has cleared the flags of the listed rows
+    // Largest value among the column's marks made before the current frontier's producer run
+    // (captures, value 0, are always among them; value-initialised brace lists leave it 0).
+    int old_hi;
 };
 
 // Candidate rows of the push-mode cop turn: a bitmap of C bits marks the configurations that

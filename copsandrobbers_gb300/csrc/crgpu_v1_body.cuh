@@ -174,6 +174,7 @@ __device__ CR_BODY_INLINE void prep_body(const V1Dev& d, int col, int nx, unsign
             if (nwk > 1) d.sync[0] = 0u;
             if (!append) {
                 const ColMeta mi = d.meta[nx];
+                mo->old_hi = max(mo->old_hi, mo->hi);
                 mo->base = (mi.hi >= mi.lo) ? mi.lo + 1 : 0;
                 mo->lo = kEmptyLo;
                 mo->hi = -1;
@@ -904,9 +905,7 @@ __device__ __forceinline__ void emit_row(const V1Dev& d, uint32_t cid, bool vali
             d.marked[((size_t)col * d.C + cid) * rwp + gl] = mm;
             t.cnt += __popc(mm ^ m);
         }
-        // column 0's frontier is consumed only through its flags and range (the last column
-        // reads column 0's marked row and table bytes), so its rows are not stored
-        if (col != 0) {
+        {
             uint32_t* frow = d.front + ((size_t)col * d.C + cid) * S * rwp;
             for (int e = gl; e < S * rwp; e += G) {
                 const int so = e / rwp, w = e - so * rwp;
@@ -1538,6 +1537,17 @@ __device__ CR_BODY_INLINE void direct_body(const V1Dev& d, int col, int nx, unsi
 //          of the transposed hop rows of those u; every other open r is complete;
 //   test  (few open r): every open r tests hop(r) within column 0's marked row.
 // Only the states found complete read column 0's table bytes (for the max).
+//
+// Fresh form, used when every older column-0 mark has a value no larger than the smallest value
+// of this pass's column-0 marks (old_hi <= lo; true on every pass measured, and the test is
+// exact either way): an open r that is complete now but was not complete before has a fresh
+// mark in hop(r), and the max over hop(r) is the largest fresh value there.  The fresh marks
+// are column 0's frontier rows, one per value slot, so per slot from the top the OR of the
+// transposed hop rows of that slot's fresh marks gives the robbers whose max is that slot's
+// value; those robbers are then tested for completeness (block or test form) and no table byte
+// is read.  An open r complete without a fresh mark in hop(r) was complete at the pass that
+// made its last mark and stayed unmarked then, so its value is at least 127 and it stays
+// unmarked; an r with empty hop(r) has value 1.
 template <bool P1, int G>
 __device__ CR_BODY_INLINE void and_body(const V1Dev& d, int col, unsigned wk, unsigned nwk) {
     extern __shared__ uint32_t sm[];
@@ -1578,6 +1588,8 @@ __device__ CR_BODY_INLINE void and_body(const V1Dev& d, int col, unsigned wk, un
         }
     }
     const int avg_deg = max(1, (nnz + n - 1) / n);
+    const int slo = mi.lo - mi.base, shi = mi.hi - mi.base;
+    const bool fresh = mi.old_hi <= mi.lo && slo >= 0 && shi < S;
     Tally t;
     const RowList rl(d, 0, mi);
     const uint32_t step = nwk * (blockDim.x >> 5) * CPW;
@@ -1601,105 +1613,218 @@ __device__ CR_BODY_INLINE void and_body(const V1Dev& d, int col, unsigned wk, un
             if (need)
                 for (int e = gl; e < S * rwp; e += G) wnew[e] = 0u;
             const int marked0 = L.sum(__popc(m0));
-            const int open = L.sum(__popc(~mc & vm));
-            const int c_test = open * (P1 ? avg_deg : rw);
-            const int c_block = (n - marked0) * rwp;
-            const int c_touch = marked0 * rwp + (P1 ? marked0 * avg_deg : open);
-            const bool touch_form = c_touch < c_test && c_touch <= c_block;
-            const bool block_form = !touch_form && c_block < c_test;
-            // block form with groups of up to 4 lanes (n <= 128): each lane walks the unmarked
-            // vertices of its own word and ORs whole rows, like the touch form; wider groups
-            // keep one pass per lane over the whole list (clustered unmarked vertices would
-            // leave a few lanes with all the rows)
             constexpr bool kBlockRows = G <= 4;
-            const bool rows_form = touch_form || (kBlockRows && block_form);
-            if (__any_sync(FULL_MASK, rows_form && need)) {
-                // each lane ORs the transposed hop rows of the marked (touch form) or unmarked
-                // (block form) vertices of its own word; the group reduces the rows by halving
-                // into wtouch: the touched, or the blocked, robbers
-                uint32_t acc[G];
+            __syncwarp();
+            if (fresh) {
+                const uint32_t open = (need && gl < rw) ? (~mc & vm) : 0u;
+                uint32_t done = 0u;   // open robbers whose hop(r) meets a fresh mark of a slot seen
+                const uint32_t* frow0 = d.front + (size_t)cid * S * rwp;
+                for (int s = shi; s >= slo; --s) {
+                    const uint32_t fs = (need && gl < rw) ? frow0[s * rwp + gl] : 0u;
+                    if (!__any_sync(FULL_MASK, fs != 0u)) continue;
+                    uint32_t acc[G];
 #pragma unroll
-                for (int i = 0; i < G; ++i) acc[i] = 0u;
-                if (rows_form && need && gl < rw) {
-                    uint32_t mb = touch_form ? m0 : (~m0 & vm);
+                    for (int i = 0; i < G; ++i) acc[i] = 0u;
+                    uint32_t mb = fs;
                     while (mb) {
-                        const int v = gl * 32 + __ffs(mb) - 1;
+                        const uint32_t* row = rhop + (size_t)(gl * 32 + __ffs(mb) - 1) * rwp;
                         mb &= mb - 1;
-                        const uint32_t* row = rhop + (size_t)v * rwp;
 #pragma unroll
                         for (int w = 0; w < G; ++w)
                             if (w < rwp) acc[w] |= row[w];
                     }
-                }
-                group_or<G, G>(acc, gl, wtouch, (rows_form && need) ? rwp : 0);
-            }
-            __syncwarp();
-            if (need && gl < rw) {
-                const uint8_t* trow = d.table + (size_t)cid * n * cols;
-                // candidates: touched and open (count form), open and not blocked (block form,
-                // all of them complete), or every open state (test form)
-                uint32_t cand = ~mc & vm;
-                if (touch_form) cand &= wtouch[gl] | CR_LDG(&d.g.isolated[gl]);
-                if (block_form) {
-                    if (kBlockRows) {
-                        cand &= ~wtouch[gl];
-                    } else {
-                        uint32_t blocked = 0;
-                        for (int w2 = 0; w2 < rw; ++w2) {
-                            uint32_t ub = ~wm0[w2] & valid_mask(n, w2);
-                            while (ub) {
-                                const int u = w2 * 32 + __ffs(ub) - 1;
-                                ub &= ub - 1;
-                                blocked |= rhop[(size_t)u * rwp + gl];
-                            }
+                    group_or<G, G>(acc, gl, wtouch, L.any(fs != 0u) ? rwp : 0);
+                    __syncwarp();
+                    if (L.any(fs != 0u) && gl < rw) {
+                        const uint32_t tw = wtouch[gl] & open & ~done;
+                        done |= tw;
+                        const int v = mi.base + s + 1;
+                        if (tw && v < kMaxRound) {
+                            const int so = v - out_base;
+                            if (so < 0 || so >= S) t.err |= kErrSlot;
+                            else wnew[so * rwp + gl] = tw;
                         }
-                        cand &= ~blocked;
                     }
+                    __syncwarp();
                 }
-                while (cand) {
-                    const int r = gl * 32 + __ffs(cand) - 1;
-                    cand &= cand - 1;
-                    const uint32_t e0 = rp[r], e1 = rp[r + 1];
-                    bool all;
-                    int mx = 0;
-                    if (P1) {
-                        if (block_form) {
-                            all = true;
-                        } else {
-                            all = true;
-                            for (uint32_t e = e0; e < e1 && all; ++e) {
+                // completeness of the touched robbers: the blocked set (OR of the transposed hop
+                // rows of the unmarked column-0 vertices) or a test per robber, whichever is cheaper
+                const int ncand = L.sum(__popc(done));
+                const bool block_form = (n - marked0) * rwp < ncand * (P1 ? avg_deg : rw);
+                const bool do_block = need && ncand > 0 && block_form;
+                uint32_t comp = done;
+                if (kBlockRows) {
+                    if (__any_sync(FULL_MASK, do_block)) {
+                        uint32_t acc[G];
+#pragma unroll
+                        for (int i = 0; i < G; ++i) acc[i] = 0u;
+                        uint32_t mb = (do_block && gl < rw) ? (~m0 & vm) : 0u;
+                        while (mb) {
+                            const uint32_t* row = rhop + (size_t)(gl * 32 + __ffs(mb) - 1) * rwp;
+                            mb &= mb - 1;
+#pragma unroll
+                            for (int w = 0; w < G; ++w)
+                                if (w < rwp) acc[w] |= row[w];
+                        }
+                        group_or<G, G>(acc, gl, wtouch, do_block ? rwp : 0);
+                        __syncwarp();
+                        if (do_block && gl < rw) comp &= ~wtouch[gl];
+                    }
+                } else if (do_block && gl < rw) {
+                    uint32_t blocked = 0;
+                    for (int w2 = 0; w2 < rw; ++w2) {
+                        uint32_t ub = ~wm0[w2] & valid_mask(n, w2);
+                        while (ub) {
+                            const int u = w2 * 32 + __ffs(ub) - 1;
+                            ub &= ub - 1;
+                            blocked |= rhop[(size_t)u * rwp + gl];
+                        }
+                    }
+                    comp &= ~blocked;
+                }
+                if (need && !block_form && gl < rw) {
+                    uint32_t c = done;
+                    comp = 0u;
+                    while (c) {
+                        const int r = gl * 32 + __ffs(c) - 1;
+                        c &= c - 1;
+                        bool all = true;
+                        if (P1) {
+                            const uint32_t e1 = rp[r + 1];
+                            for (uint32_t e = rp[r]; e < e1 && all; ++e) {
                                 const int v = adj[e];
                                 all = (wm0[v >> 5] >> (v & 31)) & 1u;
                             }
-                        }
-                        if (all)
-                            for (uint32_t e = e0; e < e1; ++e)
-                                mx = max(mx, (int)(trow[(size_t)adj[e] * cols] >> 1));
-                    } else {
-                        const uint32_t* h = d.hop + (size_t)r * rwp;
-                        all = true;
-                        if (!block_form)
+                        } else {
+                            const uint32_t* h = d.hop + (size_t)r * rwp;
                             for (int w = 0; w < rw && all; ++w) all = (CR_LDG(&h[w]) & ~wm0[w]) == 0u;
-                        if (all) {
-                            for (int w = 0; w < rw; ++w) {
-                                uint32_t b = CR_LDG(&h[w]);
-                                while (b) {
-                                    const int v = w * 32 + __ffs(b) - 1;
-                                    b &= b - 1;
-                                    mx = max(mx, (int)(trow[(size_t)v * cols] >> 1));
+                        }
+                        if (all) comp |= 1u << (r & 31);
+                    }
+                }
+                if (need && gl < rw) {
+                    for (int so = 0; so < S; ++so) wnew[so * rwp + gl] &= comp;
+                    // an open r with empty hop(r): value 1
+                    const uint32_t iso = open & CR_LDG(&d.g.isolated[gl]);
+                    if (iso) {
+                        const int so = 1 - out_base;
+                        if (so < 0 || so >= S) t.err |= kErrSlot;
+                        else wnew[so * rwp + gl] |= iso;
+                    }
+                    uint8_t* tcol = d.table + ((size_t)cid * n + gl * 32) * cols + col;
+                    for (int so = 0; so < S; ++so) {
+                        uint32_t b = wnew[so * rwp + gl];
+                        if (!b) continue;
+                        const int v = out_base + so;
+                        t.lo = min(t.lo, v);
+                        t.hi = max(t.hi, v);
+                        const uint8_t val = (uint8_t)(1 | (v << 1));
+                        while (b) {
+                            tcol[(size_t)(__ffs(b) - 1) * cols] = val;
+                            b &= b - 1;
+                        }
+                    }
+                }
+            } else {
+                const int open = L.sum(__popc(~mc & vm));
+                const int c_test = open * (P1 ? avg_deg : rw);
+                const int c_block = (n - marked0) * rwp;
+                const int c_touch = marked0 * rwp + (P1 ? marked0 * avg_deg : open);
+                const bool touch_form = c_touch < c_test && c_touch <= c_block;
+                const bool block_form = !touch_form && c_block < c_test;
+                // block form with groups of up to 4 lanes (n <= 128): each lane walks the unmarked
+                // vertices of its own word and ORs whole rows, like the touch form; wider groups
+                // keep one pass per lane over the whole list (clustered unmarked vertices would
+                // leave a few lanes with all the rows)
+                const bool rows_form = touch_form || (kBlockRows && block_form);
+                if (__any_sync(FULL_MASK, rows_form && need)) {
+                    // each lane ORs the transposed hop rows of the marked (touch form) or unmarked
+                    // (block form) vertices of its own word; the group reduces the rows by halving
+                    // into wtouch: the touched, or the blocked, robbers
+                    uint32_t acc[G];
+    #pragma unroll
+                    for (int i = 0; i < G; ++i) acc[i] = 0u;
+                    if (rows_form && need && gl < rw) {
+                        uint32_t mb = touch_form ? m0 : (~m0 & vm);
+                        while (mb) {
+                            const int v = gl * 32 + __ffs(mb) - 1;
+                            mb &= mb - 1;
+                            const uint32_t* row = rhop + (size_t)v * rwp;
+    #pragma unroll
+                            for (int w = 0; w < G; ++w)
+                                if (w < rwp) acc[w] |= row[w];
+                        }
+                    }
+                    group_or<G, G>(acc, gl, wtouch, (rows_form && need) ? rwp : 0);
+                }
+                __syncwarp();
+                if (need && gl < rw) {
+                    const uint8_t* trow = d.table + (size_t)cid * n * cols;
+                    // candidates: touched and open (count form), open and not blocked (block form,
+                    // all of them complete), or every open state (test form)
+                    uint32_t cand = ~mc & vm;
+                    if (touch_form) cand &= wtouch[gl] | CR_LDG(&d.g.isolated[gl]);
+                    if (block_form) {
+                        if (kBlockRows) {
+                            cand &= ~wtouch[gl];
+                        } else {
+                            uint32_t blocked = 0;
+                            for (int w2 = 0; w2 < rw; ++w2) {
+                                uint32_t ub = ~wm0[w2] & valid_mask(n, w2);
+                                while (ub) {
+                                    const int u = w2 * 32 + __ffs(ub) - 1;
+                                    ub &= ub - 1;
+                                    blocked |= rhop[(size_t)u * rwp + gl];
+                                }
+                            }
+                            cand &= ~blocked;
+                        }
+                    }
+                    while (cand) {
+                        const int r = gl * 32 + __ffs(cand) - 1;
+                        cand &= cand - 1;
+                        const uint32_t e0 = rp[r], e1 = rp[r + 1];
+                        bool all;
+                        int mx = 0;
+                        if (P1) {
+                            if (block_form) {
+                                all = true;
+                            } else {
+                                all = true;
+                                for (uint32_t e = e0; e < e1 && all; ++e) {
+                                    const int v = adj[e];
+                                    all = (wm0[v >> 5] >> (v & 31)) & 1u;
+                                }
+                            }
+                            if (all)
+                                for (uint32_t e = e0; e < e1; ++e)
+                                    mx = max(mx, (int)(trow[(size_t)adj[e] * cols] >> 1));
+                        } else {
+                            const uint32_t* h = d.hop + (size_t)r * rwp;
+                            all = true;
+                            if (!block_form)
+                                for (int w = 0; w < rw && all; ++w) all = (CR_LDG(&h[w]) & ~wm0[w]) == 0u;
+                            if (all) {
+                                for (int w = 0; w < rw; ++w) {
+                                    uint32_t b = CR_LDG(&h[w]);
+                                    while (b) {
+                                        const int v = w * 32 + __ffs(b) - 1;
+                                        b &= b - 1;
+                                        mx = max(mx, (int)(trow[(size_t)v * cols] >> 1));
+                                    }
                                 }
                             }
                         }
+                        if (!all) continue;
+                        const int v = mx + 1;
+                        if (v >= kMaxRound) continue;
+                        const int so = v - out_base;
+                        if (so < 0 || so >= S) { t.err |= kErrSlot; continue; }
+                        wnew[so * rwp + gl] |= 1u << (r & 31);  // this lane owns word r >> 5
+                        d.table[((size_t)cid * n + r) * cols + col] = (uint8_t)(1 | (v << 1));
+                        t.lo = min(t.lo, v);
+                        t.hi = max(t.hi, v);
                     }
-                    if (!all) continue;
-                    const int v = mx + 1;
-                    if (v >= kMaxRound) continue;
-                    const int so = v - out_base;
-                    if (so < 0 || so >= S) { t.err |= kErrSlot; continue; }
-                    wnew[so * rwp + gl] |= 1u << (r & 31);  // this lane owns word r >> 5
-                    d.table[((size_t)cid * n + r) * cols + col] = (uint8_t)(1 | (v << 1));
-                    t.lo = min(t.lo, v);
-                    t.hi = max(t.hi, v);
                 }
             }
             __syncwarp();

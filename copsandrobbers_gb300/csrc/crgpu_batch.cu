@@ -372,7 +372,7 @@ __device__ int solve_job(const BatchDev& b, unsigned char* slot, int gi, int jr,
                 cop_pull_body<K, NWP, G>(d, col, nx, 0, 1);
                 __syncthreads();
                 if (K == 3) {
-                    pair_h1_body<NWP, G>(d, nx, 0, 1);
+                    pair_h1_body(d, nx, 0, 1);
                     __syncthreads();
                     sep_pull_body<NWP, G>(d, col, nx, 0, 1);
                     __syncthreads();
@@ -501,7 +501,8 @@ size_t batch_smem(int threads, int max_n) {
         const size_t andb = (size_t)warps * CPW * and_group_words(S, rwp);
         const size_t push = (size_t)warps * S * rwp;
         const size_t pull = cop + rank_table_words(kBatchMaxK, n);
-        best = std::max(best, std::max(pull, std::max(andb, push)) * 4);
+        const size_t pair = (size_t)pair_smem_words(n);
+        best = std::max(best, std::max(std::max(pull, pair), std::max(andb, push)) * 4);
     }
     return best;
 }

@@ -75,7 +75,7 @@ template <int K, int NWP, int G>
 __global__ void __launch_bounds__(256, NWP >= 32 ? 3 : 4) k_cop_a(V1Dev d, int col, int nx) {
     cop_seed_body<K, G>(d, col, nx, blockIdx.x, gridDim.x);
     cop_push_body<K>(d, col, nx, blockIdx.x, gridDim.x);
-    if constexpr (K == 3) pair_h1_body<NWP, G>(d, nx, blockIdx.x, gridDim.x);
+    if constexpr (K == 3) pair_h1_body(d, nx, blockIdx.x, gridDim.x);
 }
 template <int K, int NWP, int G>
 __global__ void __launch_bounds__(256, NWP >= 32 ? 3 : 4) k_cop_b(V1Dev d, int col, int nx) {
@@ -158,7 +158,8 @@ template <int K, int NWP, int G>
 static void launch_cop_ng(const V1Dev& d, int col, int nx, int grid, cudaStream_t st) {
     const size_t sm = cop_smem_bytes(d.S, d.g.rwp);
     const size_t smr = sm + (size_t)rank_table_words(K, d.g.n) * 4;
-    k_cop_a<K, NWP, G><<<grid, 256, smr, st>>>(d, col, nx);
+    const size_t sma = K == 3 ? std::max(smr, (size_t)pair_smem_words(d.g.n) * 4) : smr;
+    k_cop_a<K, NWP, G><<<grid, 256, sma, st>>>(d, col, nx);
     if (!(K == 3 && d.h1)) k_cop_pull<K, NWP, G><<<grid, 256, smr, st>>>(d, col, nx);
     k_cop_b<K, NWP, G><<<grid, 256, sm, st>>>(d, col, nx);
 }

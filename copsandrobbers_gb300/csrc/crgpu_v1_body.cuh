@@ -48,6 +48,9 @@ __host__ __device__ inline int and_group_words(int S, int rwp) { return 3 * rwp 
 // Words of shared memory the pull body stages the rank table in (16-byte multiple).
 __host__ __device__ inline int rank_table_words(int k, int n) { return (k * (n + 1) + 3) & ~3; }
 
+// Words of shared memory the separable turn's pair rows stage frontier rows in (16 KB).
+constexpr int kPairStageWords = 4096;
+
 __device__ __forceinline__ bool frontier_sparse(const ColMeta& m, uint32_t C) {
     return (unsigned long long)m.rows * kPushRatio < C;
 }
@@ -1149,17 +1152,27 @@ __device__ __forceinline__ void pair_of(uint32_t q, int n, int& x, int& y) {
 //   H1[{x, y}][c] = OR over z in N(c) of F[sort(x, y, z)]             (pair_h1_body)
 //   acc(C)        = OR over x in N(c1), y in N(c2) of H1[{x, y}][c3]  (sep_pull_body)
 // so a configuration reads deg^2 rows of H1 (consecutive configurations read consecutive
-// rows) instead of ranking and gathering deg^3 successor tuples, and the ranks are taken
-// once per (pair, z) instead of once per tuple.  OR is exact, so the marks are the pull's.
-// Stage 1: a lane group per H1 row, its lanes over z in N(c), reduced by halving.
-template <int NWP, int G>
+// rows) instead of ranking and gathering deg^3 successor tuples.  OR is exact, so the marks
+// are the pull's.
+// Stage 1: a block per pair {x, y}.  Its n frontier rows F[sort(x, y, z)], z = 0 .. n-1, are
+// staged in shared memory (one rank and one row load per z; a row whose flag is clear counts
+// as empty), then every H1 row of the pair is the OR of the staged rows of N(c): the ranks
+// are taken once per (pair, z), not per (pair, c, z in N(c)), and the pair's n output rows are
+// written as one contiguous stretch.  A block takes as many consecutive pairs per round as
+// give each of its threads a unit of work (one pair for 256 threads at n = 128, four for the
+// batch kernel's 1024); rows wider than the staging area go one pair at a time in word chunks.
+__host__ __device__ inline int pair_chunk_words(int n, int S, int rwp) {
+    const int budget = kPairStageWords / n;
+    const int w = S * rwp;
+    if (w <= budget) return w;
+    return (rwp & 3) == 0 ? (budget & ~3) : budget;
+}
+__host__ __device__ inline int pair_smem_words(int n) { return rank_table_words(3, n) + kPairStageWords; }
+
 __device__ CR_BODY_INLINE void pair_h1_body(const V1Dev& d, int nx, unsigned wk, unsigned nwk) {
     extern __shared__ uint32_t sm[];
+    __shared__ uint32_t s_xy[32];
     constexpr int K = 3;
-    constexpr int CPW = 32 / G;
-    const int warp = threadIdx.x >> 5;
-    const Lanes<G> L(threadIdx.x & 31);
-    const int gl = L.glane;
     const int n = d.g.n, rwp = d.g.rwp, S = d.S;
     const ColMeta mi = d.meta[nx];
     if (!d.h1 || mi.hi < mi.lo || mi.seed || frontier_sparse(mi, d.C)) return;
@@ -1167,62 +1180,85 @@ __device__ CR_BODY_INLINE void pair_h1_body(const V1Dev& d, int nx, unsigned wk,
     const int nwords = s_used * rwp;
     const int np1 = n + 1;
     uint32_t* sB = sm;
+    uint32_t* stage = sm + rank_table_words(K, n);
     for (int i = threadIdx.x; i < K * np1; i += blockDim.x) sB[i] = CR_LDG(&d.binom[i]);
-    __syncthreads();
-    uint32_t* wacc = sm + rank_table_words(K, n) + (warp * CPW + L.grp) * (2 * S * rwp);
     const uint32_t* CR_RESTRICT fin = d.front + (size_t)nx * d.C * S * rwp;
     const uint8_t* CR_RESTRICT fflag_in = d.fflag + (size_t)nx * d.C;
     const uint32_t* CR_RESTRICT rp = cop_rows(d.g);
     const uint16_t* CR_RESTRICT adj = cop_cols(d.g);
     const bool vec4 = (rwp & 3) == 0;
+    const int U = vec4 ? 4 : 1;
+    const int wc = pair_chunk_words(n, S, rwp);
+    const size_t rstride = (size_t)S * rwp;
+    const uint32_t P = (uint32_t)(n * (n + 1) / 2);
+    // pairs per round: enough units for every thread of the block when a row is staged whole
+    int PR = 1;
+    if (wc >= nwords) {
+        PR = (int)blockDim.x / (n * (nwords / U));
+        PR = max(1, min(PR, min(32, kPairStageWords / (n * wc))));
+    }
     unsigned err = 0;
-    const size_t rows = (size_t)n * (n + 1) / 2 * n;
-    const size_t step = (size_t)nwk * (blockDim.x >> 5) * CPW;
-    for (size_t rb = ((size_t)wk * (blockDim.x >> 5) + warp) * CPW; rb < rows; rb += step) {
-        const size_t row = rb + L.grp;
-        const bool ok = row < rows;
-        uint32_t acc[NWP];
-#pragma unroll
-        for (int i = 0; i < NWP; ++i) acc[i] = 0u;
-        int x = 0, y = 0, lo = 0, dg = 0;
-        if (ok) {
-            const uint32_t q = (uint32_t)(row / n);
-            const int c = (int)(row - (size_t)q * n);
-            pair_of(q, n, x, y);
-            lo = CR_LDG(&rp[c]);
-            dg = CR_LDG(&rp[c + 1]) - lo;
+    for (uint32_t q0 = wk * PR; q0 < P; q0 += nwk * PR) {
+        const int np = (int)min((uint32_t)PR, P - q0);
+        if ((int)threadIdx.x < np) {
+            int x, y;
+            pair_of(q0 + threadIdx.x, n, x, y);
+            s_xy[threadIdx.x] = (uint32_t)x | ((uint32_t)y << 16);
         }
-        for (int t = gl; t < dg; t += G) {
-            const int z = CR_LDG(&adj[lo + t]);
-            int cc[K];
-            cc[0] = z < x ? z : x;
-            cc[1] = z < x ? x : (z < y ? z : y);
-            cc[2] = z < y ? y : z;
-            const uint32_t s = rank_s<K>(cc, sB, np1);
-            if (s >= d.C) { err |= kErrRank; continue; }
-            if (!CR_LDG(&fflag_in[s])) continue;
-            const uint32_t* fr = fin + (size_t)s * S * rwp;
-            if (vec4) {
-#pragma unroll
-                for (int w = 0; w < NWP; w += 4) {
-                    if (w < nwords) {
-                        const uint4 v = CR_LDG(reinterpret_cast<const uint4*>(fr + w));
-                        acc[w] |= v.x; acc[w + 1] |= v.y; acc[w + 2] |= v.z; acc[w + 3] |= v.w;
-                    }
+        __syncthreads();
+        uint32_t* out = d.h1 + (size_t)q0 * n * rstride;
+        for (int w0 = 0; w0 < nwords; w0 += wc) {
+            const int upr = min(wc, nwords - w0) / U;   // units (of U words) per row
+            const int per = n * upr;                    // units per pair
+            for (int i = threadIdx.x; i < np * per; i += blockDim.x) {
+                const int j = i / per, rem = i - j * per;
+                const int z = rem / upr, u = rem - z * upr;
+                const uint32_t xy = s_xy[j];
+                const int x = (int)(xy & 0xFFFFu), y = (int)(xy >> 16);
+                int cc[K];
+                cc[0] = z < x ? z : x;
+                cc[1] = z < x ? x : (z < y ? z : y);
+                cc[2] = z < y ? y : z;
+                uint32_t s = rank_s<K>(cc, sB, np1);
+                const bool bad = s >= d.C;
+                if (bad) {
+                    err |= kErrRank;
+                    s = 0;
                 }
-            } else {
-#pragma unroll
-                for (int w = 0; w < NWP; ++w)
-                    if (w < nwords) acc[w] |= CR_LDG(fr + w);
+                const bool live = !bad && CR_LDG(&fflag_in[s]) != 0;
+                const uint32_t* src = fin + (size_t)s * rstride + w0 + u * U;
+                uint32_t* dst = stage + (j * n + z) * wc + u * U;
+                if (vec4) {
+                    uint4 v = CR_LDG(reinterpret_cast<const uint4*>(src));
+                    if (!live) v = make_uint4(0u, 0u, 0u, 0u);
+                    *reinterpret_cast<uint4*>(dst) = v;
+                } else {
+                    const uint32_t v = CR_LDG(src);
+                    dst[0] = live ? v : 0u;
+                }
             }
+            __syncthreads();
+            for (int i = threadIdx.x; i < np * per; i += blockDim.x) {
+                const int j = i / per, rem = i - j * per;
+                const int c = rem / upr, u = rem - c * upr;
+                const uint32_t e1 = CR_LDG(&rp[c + 1]);
+                const uint32_t* sj = stage + j * n * wc + u * U;
+                uint32_t* o = out + ((size_t)j * n + c) * rstride + w0 + u * U;
+                if (vec4) {
+                    uint4 a = make_uint4(0u, 0u, 0u, 0u);
+                    for (uint32_t e = CR_LDG(&rp[c]); e < e1; ++e) {
+                        const uint4 v = *reinterpret_cast<const uint4*>(sj + CR_LDG(&adj[e]) * wc);
+                        a.x |= v.x; a.y |= v.y; a.z |= v.z; a.w |= v.w;
+                    }
+                    *reinterpret_cast<uint4*>(o) = a;
+                } else {
+                    uint32_t a = 0u;
+                    for (uint32_t e = CR_LDG(&rp[c]); e < e1; ++e) a |= sj[CR_LDG(&adj[e]) * wc];
+                    o[0] = a;
+                }
+            }
+            __syncthreads();
         }
-        group_or<NWP, G>(acc, gl, wacc, ok ? nwords : 0);
-        __syncwarp();
-        if (ok) {
-            uint32_t* out = d.h1 + row * S * rwp;
-            for (int e = gl; e < nwords; e += G) out[e] = wacc[e];
-        }
-        __syncwarp();
     }
     err = __reduce_or_sync(FULL_MASK, err);
     if ((threadIdx.x & 31) == 0 && err) atomicOr(d.err, err);

@@ -1608,7 +1608,11 @@ __device__ CR_BODY_INLINE void and_body(const V1Dev& d, int col, unsigned wk, un
     const uint16_t* adj = d.g.col;
     const uint32_t* rhop = d.g.rhop;
     const int nnz = (int)rp[n];
-    if (d.and_stage_words) {
+    const RowList rl(d, 0, mi);
+    const uint32_t step = nwk * (blockDim.x >> 5) * CPW;
+    if (wk * (blockDim.x >> 5) * CPW >= rl.n) return;   // no row for this block
+    // staging pays off only when each lane group takes a few rows
+    if (d.and_stage_words && rl.n >= 2u * step) {
         const uint32_t need = (uint32_t)(n * rwp + n + 1) + (uint32_t)(nnz + 1) / 2;
         if (need <= d.and_stage_words) {
             uint32_t* st = sm + (blockDim.x >> 5) * CPW * per_grp;
@@ -1627,8 +1631,6 @@ __device__ CR_BODY_INLINE void and_body(const V1Dev& d, int col, unsigned wk, un
     const int slo = mi.lo - mi.base, shi = mi.hi - mi.base;
     const bool fresh = mi.old_hi <= mi.lo && slo >= 0 && shi < S;
     Tally t;
-    const RowList rl(d, 0, mi);
-    const uint32_t step = nwk * (blockDim.x >> 5) * CPW;
     for (uint32_t b0 = (wk * (blockDim.x >> 5) + warp) * CPW; b0 < rl.n; b0 += step) {
         {
             const uint32_t li = b0 + L.grp;

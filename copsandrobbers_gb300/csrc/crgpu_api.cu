@@ -17,7 +17,7 @@
 
 namespace crgpu {
 void launch_cop(const V1Dev& d, int col, int nx, int direct, int grid, cudaStream_t st);
-void launch_and(const V1Dev& d, int col, bool p1, int grid, cudaStream_t st);
+void launch_and(const V1Dev& d, int col, bool p1, int grid, cudaStream_t st, const LoopCtl* loop = nullptr);
 void launch_prep(const V1Dev& d, int col, int nx, int grid, cudaStream_t st);
 void launch_init(const V1Dev& d, int grid, cudaStream_t st);
 void launch_init_pass1(const V1Dev& d, int num_sms, cudaStream_t st);
@@ -28,10 +28,7 @@ void launch_game(const uint8_t* table, const uint16_t* configs, const unsigned l
                  const unsigned long long* trans, const uint32_t* rp, const uint16_t* adj, int n, int k,
                  long long best, int cap, long long* out_c, int* out_r, int* count, int* captured,
                  cudaStream_t st);
-void launch_loop_start(const unsigned long long* counters, unsigned long long* hist, const int* idx,
-                       const unsigned* err, cudaGraphConditionalHandle loop, cudaStream_t st);
-void launch_pass_end(const unsigned long long* counters, unsigned long long* hist, int* idx, int cap,
-                     const unsigned* err, cudaGraphConditionalHandle loop, cudaStream_t st);
+void launch_loop_enter(const V1Dev& d, const LoopCtl& c, int grid, cudaStream_t st);
 void launch_verdict(const V1Dev& d, int cols, unsigned long long* best, int grid, cudaStream_t st);
 void launch_popcount(const uint32_t* plane, size_t words, unsigned long long* out, int grid,
                      cudaStream_t st);
@@ -670,9 +667,10 @@ static int v1_init_pass1_enqueue(cr_solver* s) {
     cudaStream_t st = ctx->stream;
     CR_CUDA(ctx, cudaMemsetAsync(s->d_counters, 0, 4 * sizeof(unsigned long long), st));
     CR_CUDA(ctx, cudaMemsetAsync(s->d_err, 0, sizeof(unsigned), st));
-    // column 0's frontier after pass 1 is every row (the implicit list); column 1's list is
-    // built from its flags after the kernel
-    ColMeta meta[2] = {ColMeta{0, 0, 0, 0, (int)std::min<uint64_t>(s->C, INT32_MAX), 0, -1, 0},
+    // column 0's frontier after pass 1 is every row (the implicit list), already consumed by
+    // the fused last column, which leaves its flags clear; column 1's list is built from its
+    // flags after the kernel
+    ColMeta meta[2] = {ColMeta{0, 0, 0, 0, (int)std::min<uint64_t>(s->C, INT32_MAX), 0, -1, 1},
                        ColMeta{1, kEmptyLo, -1, 0, 0, 0, 0, 0}};
     CR_CUDA(ctx, cudaMemsetAsync(s->d_sync, 0, 2 * sizeof(unsigned), st));
     CR_CUDA(ctx, cudaMemcpyAsync(s->d_meta, meta, sizeof(meta), cudaMemcpyHostToDevice, st));
@@ -716,13 +714,15 @@ static int materialize_init(cr_solver* s) {
 }
 
 // Enqueue one pass: per column a prep kernel and its producer, then the pass counter copy.
-static int v1_enqueue_pass(cr_solver* s, bool profile, bool readback = true) {
+// Inside the device-side pass loop (loop set) the last column also ends the pass and runs
+// column 0's prep for the next one, so the pass starts with column 0's producer.
+static int v1_enqueue_pass(cr_solver* s, bool profile, bool readback = true, const LoopCtl* loop = nullptr) {
     cr_context* ctx = s->ctx;
     cudaStream_t st = ctx->stream;
     V1Dev d = dev_view(s);
     for (int col = 0; col < s->cols; ++col) {
         const int nx = (col + 1) % s->cols;
-        launch_prep(d, col, nx, s->grid_small, st);
+        if (!(loop && col == 0)) launch_prep(d, col, nx, s->grid_small, st);
         if (col % 2 == 0) {
             if (profile) CR_CUDA(ctx, cudaEventRecord(s->evc0, st));
             launch_cop(d, col, nx, 0, s->grid_cop, st);
@@ -730,7 +730,7 @@ static int v1_enqueue_pass(cr_solver* s, bool profile, bool readback = true) {
         } else if (col < s->cols - 1) {
             launch_cop(d, col, nx, 1, s->grid_cop, st);
         } else {
-            launch_and(d, col, s->p == 1, s->grid_cop, st);
+            launch_and(d, col, s->p == 1, s->grid_cop, st, loop);
         }
         CR_CUDA(ctx, cudaGetLastError());
         if (profile && col % 2 == 0) {
@@ -884,8 +884,8 @@ int cr_solver_pass(cr_solver* s, uint64_t* new_wins) {
 
 static constexpr int kHistCap = 1 << 16;   // passes one device-side loop may run
 
-// The pass loop graph: k_loop_start; WHILE (flag) { one pass; k_pass_end }, the flag set by
-// k_loop_start and then by each k_pass_end.
+// The pass loop graph: k_loop_enter; WHILE (flag) { one pass, ending in k_and_end }, the flag
+// set by k_loop_enter and then by each pass's last column.
 static int build_run_graph(cr_solver* s) {
     cr_context* ctx = s->ctx;
     cudaStream_t st = ctx->stream;
@@ -897,11 +897,13 @@ static int build_run_graph(cr_solver* s) {
     CR_CUDA(ctx, cudaGraphCreate(&g, 0));
     cudaGraphConditionalHandle loop;
     cudaError_t e = cudaGraphConditionalHandleCreate(&loop, g, 0, cudaGraphCondAssignDefault);
+    const LoopCtl ctl{s->d_hist, s->d_hist_n, kHistCap, loop};
+    const V1Dev d = dev_view(s);
     // the start node sets the loop condition (and records a first pass run just before)
     cudaGraphNode_t start = nullptr;
     if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(st, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        launch_loop_start(s->d_counters, s->d_hist, s->d_hist_n, s->d_err, loop, st);
+        launch_loop_enter(d, ctl, s->grid_small, st);
         cudaGraph_t same = nullptr;
         e = cudaStreamEndCapture(st, &same);
     }
@@ -918,8 +920,7 @@ static int build_run_graph(cr_solver* s) {
     if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(st, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
                                                             cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        int rc = v1_enqueue_pass(s, false, false);
-        launch_pass_end(s->d_counters, s->d_hist, s->d_hist_n, kHistCap, s->d_err, loop, st);
+        int rc = v1_enqueue_pass(s, false, false, &ctl);
         cudaGraph_t body = nullptr;
         e = cudaStreamEndCapture(st, &body);
         if (rc) {
@@ -977,10 +978,10 @@ static int v1_run_on_device(cr_solver* s) {
                                 cudaMemcpyDeviceToHost));
     }
     const int loop_passes = first ? n - 1 : n;
-    int per_pass = s->cols + 1;  // prep kernels and the loop's pass end
+    int per_pass = s->cols - 1;  // prep kernels (column 0's runs in the previous pass's last column)
     for (int col = 0; col < s->cols; ++col)
         per_pass += col % 2 == 0 ? cop_launches_k(0, s->k, s->d_h1 != nullptr) : (col < s->cols - 1 ? cop_launches(1) : 1);
-    s->stats.kernel_launches += (int64_t)per_pass * loop_passes + 1;   // and the loop's start
+    s->stats.kernel_launches += (int64_t)per_pass * loop_passes + 1;   // and the loop's entry
     if (bits & kErrRank) return fail(ctx, CR_ERR_INTERNAL, "successor rank out of range");
     if (bits & kErrSlot) {
         // the last pass overflowed its value slots: keep the passes before it, widen the slots

@@ -329,7 +329,7 @@ __device__ int solve_job(const BatchDev& b, unsigned char* slot, int gi, int jr,
         build_cover(d, slot + L.cover, maxdeg);
         if (threadIdx.x == 0) {
             for (int c = 0; c < cols; ++c) d.meta[c] = ColMeta{0, kEmptyLo, -1, 0, 0, 0, 0, 0};
-            d.meta[0] = ColMeta{0, 0, 0, 0, (int)C, 0, -1, 0};
+            d.meta[0] = ColMeta{0, 0, 0, 0, (int)C, 0, -1, 1};   // consumed: flags left clear
             d.meta[1] = ColMeta{1, kEmptyLo, -1, 0, 0, 0, 0, 0};
         }
         __syncthreads();

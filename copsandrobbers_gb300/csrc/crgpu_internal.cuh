@@ -115,6 +115,15 @@ struct V1Dev {
     unsigned int* err;
 };
 
+// Bookkeeping of a device-side pass loop: the history of pass counts, its length and capacity,
+// and the WHILE node's condition.
+struct LoopCtl {
+    unsigned long long* hist;
+    int* idx;
+    int cap;
+    cudaGraphConditionalHandle loop;
+};
+
 __host__ __device__ inline int round_words(int rw) { return rw <= 2 ? rw : (rw + 3) & ~3; }
 
 // Raises a kernel's dynamic shared-memory limit to at least `bytes` and never lowers it.  The

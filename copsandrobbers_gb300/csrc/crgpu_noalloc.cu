@@ -35,7 +35,7 @@
 
 namespace crgpu {
 void launch_cop(const V1Dev& d, int col, int nx, int direct, int grid, cudaStream_t st);
-void launch_and(const V1Dev& d, int col, bool p1, int grid, cudaStream_t st);
+void launch_and(const V1Dev& d, int col, bool p1, int grid, cudaStream_t st, const LoopCtl* loop = nullptr);
 void launch_prep(const V1Dev& d, int col, int nx, int grid, cudaStream_t st);
 void launch_init(const V1Dev& d, int grid, cudaStream_t st);
 void launch_unrank(const uint32_t* B, int n, int k, uint32_t C, uint16_t* out, int grid, cudaStream_t st);

@@ -92,43 +92,46 @@ template <bool P1, int G>
 __global__ void __launch_bounds__(256, 4) k_and(V1Dev d, int col) {
     and_body<P1, G>(d, col, blockIdx.x, gridDim.x);
 }
+// The last column inside the device-side pass loop, with the loop's bookkeeping in its last
+// block: the pass's count joins the history, the loop goes on while the pass found something
+// (no error bit, history not full), and column 0's prep for the next pass runs (this column
+// cleared every flag of column 0's list, so that prep is a reset of the column's state).
+template <bool P1, int G>
+__global__ void __launch_bounds__(256, 4) k_and_end(V1Dev d, int col, LoopCtl c) {
+    and_body<P1, G>(d, col, blockIdx.x, gridDim.x);
+    __syncthreads();
+    if (threadIdx.x == 0 && grid_last_block(d, gridDim.x)) {
+        const int i = *c.idx;
+        const unsigned long long f = *d.pass_new;
+        c.hist[i] = f;
+        *c.idx = i + 1;
+        cudaGraphSetConditional(c.loop, (f != 0ull && *d.err == 0u && i + 1 < c.cap) ? 1u : 0u);
+        prep_reset(d, 0, 1);
+    }
+}
+
+// Entry of the device-side pass loop: column 0's prep for the first pass of the loop; its last
+// block records a first pass run just before the loop (*idx = 1, set by the host) as the
+// history's first entry and starts the loop if the last pass found something and no error bit
+// is set.
+__global__ void k_loop_enter(V1Dev d, LoopCtl c) {
+    prep_clear(d, 0, blockIdx.x, gridDim.x);
+    __syncthreads();
+    if (threadIdx.x == 0 && grid_last_block(d, gridDim.x)) {
+        const unsigned long long f = *d.pass_new;
+        if (*c.idx == 1) c.hist[0] = f;
+        cudaGraphSetConditional(c.loop, (f != 0ull && *d.err == 0u) ? 1u : 0u);
+        prep_reset(d, 0, 1);
+    }
+}
+
 __global__ void k_verdict(const uint8_t* __restrict__ table, const uint32_t* __restrict__ m0,
                           uint32_t C, int n, int rw, int rwp, int cols, unsigned long long* best) {
     verdict_body(table, m0, C, n, rw, rwp, cols, best, blockIdx.x, gridDim.x);
 }
 
-// End of one pass of a device-side pass loop: append the pass count to the history and keep
-// looping while the pass found something, no error bit is set and the history has room.
-__global__ void k_pass_end(const unsigned long long* counters, unsigned long long* hist, int* idx,
-                           int cap, const unsigned* err, cudaGraphConditionalHandle loop) {
-    const int i = *idx;
-    const unsigned long long f = counters[0];
-    hist[i] = f;
-    *idx = i + 1;
-    cudaGraphSetConditional(loop, (f != 0ull && *err == 0u && i + 1 < cap) ? 1u : 0u);
-}
-
-// Start of a device-side pass loop: when the first pass ran just before the loop (*idx = 1,
-// set by the host) record its count as the history's first entry; loop while the last pass
-// found something and no error bit is set.
-__global__ void k_loop_start(const unsigned long long* counters, unsigned long long* hist, const int* idx,
-                             const unsigned* err, cudaGraphConditionalHandle loop) {
-    const unsigned long long f = counters[0];
-    if (*idx == 1) hist[0] = f;
-    cudaGraphSetConditional(loop, (f != 0ull && *err == 0u) ? 1u : 0u);
-}
-
 // ---------------------------------------------------------------- host-side launchers ---
 
-void launch_loop_start(const unsigned long long* counters, unsigned long long* hist, const int* idx,
-                       const unsigned* err, cudaGraphConditionalHandle loop, cudaStream_t st) {
-    k_loop_start<<<1, 1, 0, st>>>(counters, hist, idx, err, loop);
-}
-
-void launch_pass_end(const unsigned long long* counters, unsigned long long* hist, int* idx, int cap,
-                     const unsigned* err, cudaGraphConditionalHandle loop, cudaStream_t st) {
-    k_pass_end<<<1, 1, 0, st>>>(counters, hist, idx, cap, err, loop);
-}
 
 
 // Lanes per configuration: a power of two covering the robber row (at least 4).
@@ -219,8 +222,14 @@ size_t and_stage_words(int n, int rwp, int nnz) {
     return (size_t)n * rwp + n + 1 + (size_t)(nnz + 1) / 2;
 }
 
+template <bool P1, int G>
+static void launch_and_g(const V1Dev& d, int col, int grid, size_t sm, cudaStream_t st, const LoopCtl* loop) {
+    if (loop) k_and_end<P1, G><<<grid, 256, sm, st>>>(d, col, *loop);
+    else k_and<P1, G><<<grid, 256, sm, st>>>(d, col);
+}
+
 template <bool P1>
-static void launch_and_p(const V1Dev& d0, int col, int grid, cudaStream_t st) {
+static void launch_and_p(const V1Dev& d0, int col, int grid, cudaStream_t st, const LoopCtl* loop) {
     V1Dev d = d0;
     size_t sm = and_smem_bytes(d.S, d.g.rwp, d.g.n);
     d.and_stage_words = 0;
@@ -232,16 +241,20 @@ static void launch_and_p(const V1Dev& d0, int col, int grid, cudaStream_t st) {
         }
     }
     switch (group_lanes(d.g.rwp)) {
-        case 4: k_and<P1, 4><<<grid, 256, sm, st>>>(d, col); break;
-        case 8: k_and<P1, 8><<<grid, 256, sm, st>>>(d, col); break;
-        case 16: k_and<P1, 16><<<grid, 256, sm, st>>>(d, col); break;
-        default: k_and<P1, 32><<<grid, 256, sm, st>>>(d, col); break;
+        case 4: launch_and_g<P1, 4>(d, col, grid, sm, st, loop); break;
+        case 8: launch_and_g<P1, 8>(d, col, grid, sm, st, loop); break;
+        case 16: launch_and_g<P1, 16>(d, col, grid, sm, st, loop); break;
+        default: launch_and_g<P1, 32>(d, col, grid, sm, st, loop); break;
     }
 }
 
-void launch_and(const V1Dev& d, int col, bool p1, int grid, cudaStream_t st) {
-    if (p1) launch_and_p<true>(d, col, grid, st);
-    else launch_and_p<false>(d, col, grid, st);
+void launch_and(const V1Dev& d, int col, bool p1, int grid, cudaStream_t st, const LoopCtl* loop) {
+    if (p1) launch_and_p<true>(d, col, grid, st, loop);
+    else launch_and_p<false>(d, col, grid, st, loop);
+}
+
+void launch_loop_enter(const V1Dev& d, const LoopCtl& c, int grid, cudaStream_t st) {
+    k_loop_enter<<<grid, 256, 0, st>>>(d, c);
 }
 
 void launch_prep(const V1Dev& d, int col, int nx, int grid, cudaStream_t st) {

@@ -147,10 +147,9 @@ struct Tally {
 // frontier already holds the capture seeds).  Before an odd column it also clears the candidate
 // rows of the push-mode cop turn just run.  Every block reads the column's state first; the
 // last block to finish (counted in sync[0]) resets it, so no block reads a half-reset state.
-__device__ CR_BODY_INLINE void prep_body(const V1Dev& d, int col, int nx, unsigned wk, unsigned nwk) {
-    ColMeta* mo = d.meta + col;
-    const int append = mo->append, clean = mo->clean;
-    if (!append && !clean) {
+__device__ CR_BODY_INLINE void prep_clear(const V1Dev& d, int col, unsigned wk, unsigned nwk) {
+    const ColMeta* mo = d.meta + col;
+    if (!mo->append && !mo->clean) {
         uint8_t* f = d.fflag + (size_t)col * d.C;
         for (size_t i = (size_t)wk * blockDim.x + threadIdx.x; i < d.C; i += (size_t)nwk * blockDim.x)
             f[i] = 0;
@@ -165,32 +164,46 @@ __device__ CR_BODY_INLINE void prep_body(const V1Dev& d, int col, int nx, unsign
             if (e == 0) d.cbits[cid >> 5] = 0u;
         }
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        bool last = nwk == 1;
-        if (!last) {
-            __threadfence();
-            last = atomicAdd(&d.sync[0], 1u) == nwk - 1;
-        }
-        if (last) {
-            __threadfence();
-            if (nwk > 1) d.sync[0] = 0u;
-            if (!append) {
-                const ColMeta mi = d.meta[nx];
-                mo->old_hi = max(mo->old_hi, mo->hi);
-                mo->base = (mi.hi >= mi.lo) ? mi.lo + 1 : 0;
-                mo->lo = kEmptyLo;
-                mo->hi = -1;
-                mo->rows = 0;
-                mo->len = 0;
-                mo->clean = 0;
-            }
-            mo->seed = 0;
-            if (col == 0) *d.pass_new = 0ull;
-            if (col % 2 == 0) d.sync[1] = 0u;                // the push form's candidate list
-            if (col == d.cols - 1) d.meta[0].append = 0;   // column 0's seeded frontier is consumed
-        }
+}
+
+// Thread 0 of each block of a grid (after the block's work and a __syncthreads): true in the
+// last block to arrive, counted in sync[0], which it resets.
+__device__ __forceinline__ bool grid_last_block(const V1Dev& d, unsigned nwk) {
+    bool last = nwk == 1;
+    if (!last) {
+        __threadfence();
+        last = atomicAdd(&d.sync[0], 1u) == nwk - 1;
     }
+    if (last) {
+        __threadfence();
+        if (nwk > 1) d.sync[0] = 0u;
+    }
+    return last;
+}
+
+// The column state reset of prep, done once (the last block).
+__device__ CR_BODY_INLINE void prep_reset(const V1Dev& d, int col, int nx) {
+    ColMeta* mo = d.meta + col;
+    if (!mo->append) {
+        const ColMeta mi = d.meta[nx];
+        mo->old_hi = max(mo->old_hi, mo->hi);
+        mo->base = (mi.hi >= mi.lo) ? mi.lo + 1 : 0;
+        mo->lo = kEmptyLo;
+        mo->hi = -1;
+        mo->rows = 0;
+        mo->len = 0;
+        mo->clean = 0;
+    }
+    mo->seed = 0;
+    if (col == 0) *d.pass_new = 0ull;
+    if (col % 2 == 0) d.sync[1] = 0u;                // the push form's candidate list
+    if (col == d.cols - 1) d.meta[0].append = 0;   // column 0's seeded frontier is consumed
+}
+
+__device__ CR_BODY_INLINE void prep_body(const V1Dev& d, int col, int nx, unsigned wk, unsigned nwk) {
+    prep_clear(d, col, wk, nwk);
+    __syncthreads();
+    if (threadIdx.x == 0 && grid_last_block(d, nwk)) prep_reset(d, col, nx);
 }
 
 // The row list of a column's frontier as a consumer sees it: n entries, entry i = row id(i).
@@ -446,10 +459,11 @@ __device__ CR_BODY_INLINE void init_pass1_single(const V1Dev& d, unsigned wk, un
     // fast form: lane 4w writes word w of the column-0 marked row, lane 4w + 1 that of column 1
     const bool mwriter = (lane & 3) < 2 && (FULL || wi < rw);
     const size_t mplane = (lane & 1) ? (size_t)C * rwp : 0;
-    // the flag planes of this warp's configurations: column 0 set (every row holds captures),
-    // column 1 clear (set below for the rows that gain marks)
+    // the flag planes of this warp's configurations: column 0 clear (its frontier, every row,
+    // is consumed by the last column fused here, so the column starts pass 2 clean), column 1
+    // clear (set below for the rows that gain marks)
     for (size_t i = cb + lane; i < ce; i += 32) {
-        d.fflag[i] = 1;
+        d.fflag[i] = 0;
         d.fflag[(size_t)C + i] = 0;
     }
     __syncwarp();
@@ -831,7 +845,7 @@ __device__ CR_BODY_INLINE void init_pass1_body(const V1Dev& d, unsigned wk, unsi
             for (int e = 2 * rwp + lane; e < frow_words; e += 32) frow[e] = 0u;
         }
         if (lane == 0) {
-            *fl0 = 1;
+            *fl0 = 0;   // column 0's frontier is consumed here (the fused last column)
             *fl1 = changed ? 1 : 0;
             rows1 += changed ? 1u : 0u;
         }

@@ -16,7 +16,7 @@
 #include "crgpu_v2.h"
 
 namespace crgpu {
-void launch_cop(const V1Dev& d, int col, int nx, int direct, int grid, cudaStream_t st);
+void launch_cop(const V1Dev& d, int col, int nx, int direct, int grid, cudaStream_t st, bool end = false);
 void launch_and(const V1Dev& d, int col, bool p1, int grid, cudaStream_t st, const LoopCtl* loop = nullptr);
 void launch_prep(const V1Dev& d, int col, int nx, int grid, cudaStream_t st);
 void launch_init(const V1Dev& d, int grid, cudaStream_t st);
@@ -715,17 +715,19 @@ static int materialize_init(cr_solver* s) {
 
 // Enqueue one pass: per column a prep kernel and its producer, then the pass counter copy.
 // Inside the device-side pass loop (loop set) the last column also ends the pass and runs
-// column 0's prep for the next one, so the pass starts with column 0's producer.
+// column 0's prep for the next one, so the pass starts with column 0's producer; with p = 1
+// the last column's prep rides on the cop turn's second launch and the last column itself.
 static int v1_enqueue_pass(cr_solver* s, bool profile, bool readback = true, const LoopCtl* loop = nullptr) {
     cr_context* ctx = s->ctx;
     cudaStream_t st = ctx->stream;
     V1Dev d = dev_view(s);
+    const bool fuse1 = loop && loop->fused_prep1;
     for (int col = 0; col < s->cols; ++col) {
         const int nx = (col + 1) % s->cols;
-        if (!(loop && col == 0)) launch_prep(d, col, nx, s->grid_small, st);
+        if (!(loop && col == 0) && !(fuse1 && col == 1)) launch_prep(d, col, nx, s->grid_small, st);
         if (col % 2 == 0) {
             if (profile) CR_CUDA(ctx, cudaEventRecord(s->evc0, st));
-            launch_cop(d, col, nx, 0, s->grid_cop, st);
+            launch_cop(d, col, nx, 0, s->grid_cop, st, fuse1 && col == 0);
             if (profile) CR_CUDA(ctx, cudaEventRecord(s->evc1, st));
         } else if (col < s->cols - 1) {
             launch_cop(d, col, nx, 1, s->grid_cop, st);
@@ -897,7 +899,7 @@ static int build_run_graph(cr_solver* s) {
     CR_CUDA(ctx, cudaGraphCreate(&g, 0));
     cudaGraphConditionalHandle loop;
     cudaError_t e = cudaGraphConditionalHandleCreate(&loop, g, 0, cudaGraphCondAssignDefault);
-    const LoopCtl ctl{s->d_hist, s->d_hist_n, kHistCap, loop};
+    const LoopCtl ctl{s->d_hist, s->d_hist_n, kHistCap, loop, s->cols == 2 ? 1 : 0};
     const V1Dev d = dev_view(s);
     // the start node sets the loop condition (and records a first pass run just before)
     cudaGraphNode_t start = nullptr;
@@ -978,7 +980,9 @@ static int v1_run_on_device(cr_solver* s) {
                                 cudaMemcpyDeviceToHost));
     }
     const int loop_passes = first ? n - 1 : n;
-    int per_pass = s->cols - 1;  // prep kernels (column 0's runs in the previous pass's last column)
+    // prep kernels: column 0's runs in the previous pass's last column, and with p = 1 the last
+    // column's in the cop turn and the last column
+    int per_pass = s->cols == 2 ? 0 : s->cols - 1;
     for (int col = 0; col < s->cols; ++col)
         per_pass += col % 2 == 0 ? cop_launches_k(0, s->k, s->d_h1 != nullptr) : (col < s->cols - 1 ? cop_launches(1) : 1);
     s->stats.kernel_launches += (int64_t)per_pass * loop_passes + 1;   // and the loop's entry

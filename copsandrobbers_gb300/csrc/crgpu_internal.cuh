@@ -122,6 +122,9 @@ struct LoopCtl {
     int* idx;
     int cap;
     cudaGraphConditionalHandle loop;
+    // p = 1: the last column's prep is split between the cop turn's second launch (column 1's
+    // flags and state) and the last column itself (the push form's candidate rows)
+    int fused_prep1;
 };
 
 __host__ __device__ inline int round_words(int rw) { return rw <= 2 ? rw : (rw + 3) & ~3; }

@@ -34,7 +34,7 @@
 #include "crgpu_internal.cuh"
 
 namespace crgpu {
-void launch_cop(const V1Dev& d, int col, int nx, int direct, int grid, cudaStream_t st);
+void launch_cop(const V1Dev& d, int col, int nx, int direct, int grid, cudaStream_t st, bool end = false);
 void launch_and(const V1Dev& d, int col, bool p1, int grid, cudaStream_t st, const LoopCtl* loop = nullptr);
 void launch_prep(const V1Dev& d, int col, int nx, int grid, cudaStream_t st);
 void launch_init(const V1Dev& d, int grid, cudaStream_t st);

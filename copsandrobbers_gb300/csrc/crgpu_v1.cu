@@ -82,6 +82,17 @@ __global__ void __launch_bounds__(256, NWP >= 32 ? 3 : 4) k_cop_b(V1Dev d, int c
     if constexpr (K == 3) sep_pull_body<NWP, G>(d, col, nx, blockIdx.x, gridDim.x);
     cop_apply_body<G>(d, col, nx, blockIdx.x, gridDim.x);
 }
+// k_cop_b inside the device-side pass loop of a p = 1 solve, followed by the last column's prep
+// (column nx = 1): the flags a dense turn left in column 1 (no body of this launch reads them),
+// and in the last block the column's state reset.  The candidate rows wait for the last column.
+template <int K, int NWP, int G>
+__global__ void __launch_bounds__(256, NWP >= 32 ? 3 : 4) k_cop_b_end(V1Dev d, int col, int nx) {
+    if constexpr (K == 3) sep_pull_body<NWP, G>(d, col, nx, blockIdx.x, gridDim.x);
+    cop_apply_body<G>(d, col, nx, blockIdx.x, gridDim.x);
+    prep_clear_flags(d, nx, blockIdx.x, gridDim.x);
+    __syncthreads();
+    if (threadIdx.x == 0 && grid_last_block(d, gridDim.x)) prep_reset(d, nx, col);
+}
 template <int G>
 __global__ void __launch_bounds__(256) k_direct(V1Dev d, int col, int nx) {
     direct_body<G>(d, col, nx, blockIdx.x, gridDim.x);
@@ -98,6 +109,7 @@ __global__ void __launch_bounds__(256, 4) k_and(V1Dev d, int col) {
 // cleared every flag of column 0's list, so that prep is a reset of the column's state).
 template <bool P1, int G>
 __global__ void __launch_bounds__(256, 4) k_and_end(V1Dev d, int col, LoopCtl c) {
+    if (c.fused_prep1) prep_clear_cand(d, blockIdx.x, gridDim.x);   // this column's prep, the rest
     and_body<P1, G>(d, col, blockIdx.x, gridDim.x);
     __syncthreads();
     if (threadIdx.x == 0 && grid_last_block(d, gridDim.x)) {
@@ -158,31 +170,32 @@ static int pull_words(int S, int rwp) {
 bool pull_supported(int S, int rwp) { return pull_words(S, rwp) <= 32 && group_lanes(rwp) <= 32; }
 
 template <int K, int NWP, int G>
-static void launch_cop_ng(const V1Dev& d, int col, int nx, int grid, cudaStream_t st) {
+static void launch_cop_ng(const V1Dev& d, int col, int nx, int grid, cudaStream_t st, bool end) {
     const size_t sm = cop_smem_bytes(d.S, d.g.rwp);
     const size_t smr = sm + (size_t)rank_table_words(K, d.g.n) * 4;
     const size_t sma = K == 3 ? std::max(smr, (size_t)pair_smem_words(d.g.n) * 4) : smr;
     k_cop_a<K, NWP, G><<<grid, 256, sma, st>>>(d, col, nx);
     if (!(K == 3 && d.h1)) k_cop_pull<K, NWP, G><<<grid, 256, smr, st>>>(d, col, nx);
-    k_cop_b<K, NWP, G><<<grid, 256, sm, st>>>(d, col, nx);
+    if (end) k_cop_b_end<K, NWP, G><<<grid, 256, sm, st>>>(d, col, nx);
+    else k_cop_b<K, NWP, G><<<grid, 256, sm, st>>>(d, col, nx);
 }
 
 // Accumulator words and lanes per configuration, as the pull and the separable turn use them.
 template <int K>
-static void launch_cop_k(const V1Dev& d, int col, int nx, int grid, cudaStream_t st) {
+static void launch_cop_k(const V1Dev& d, int col, int nx, int grid, cudaStream_t st, bool end) {
     const int G = group_lanes(d.g.rwp);
     switch (pull_words(d.S, d.g.rwp)) {
-        case 2: launch_cop_ng<K, 2, 4>(d, col, nx, grid, st); break;
-        case 4: launch_cop_ng<K, 4, 4>(d, col, nx, grid, st); break;
-        case 8: launch_cop_ng<K, 8, 4>(d, col, nx, grid, st); break;
+        case 2: launch_cop_ng<K, 2, 4>(d, col, nx, grid, st, end); break;
+        case 4: launch_cop_ng<K, 4, 4>(d, col, nx, grid, st, end); break;
+        case 8: launch_cop_ng<K, 8, 4>(d, col, nx, grid, st, end); break;
         case 16:
-            if (G == 4) launch_cop_ng<K, 16, 4>(d, col, nx, grid, st);
-            else launch_cop_ng<K, 16, 8>(d, col, nx, grid, st);
+            if (G == 4) launch_cop_ng<K, 16, 4>(d, col, nx, grid, st, end);
+            else launch_cop_ng<K, 16, 8>(d, col, nx, grid, st, end);
             break;
         default:
-            if (G == 4) launch_cop_ng<K, 32, 4>(d, col, nx, grid, st);
-            else if (G == 8) launch_cop_ng<K, 32, 8>(d, col, nx, grid, st);
-            else launch_cop_ng<K, 32, 16>(d, col, nx, grid, st);
+            if (G == 4) launch_cop_ng<K, 32, 4>(d, col, nx, grid, st, end);
+            else if (G == 8) launch_cop_ng<K, 32, 8>(d, col, nx, grid, st, end);
+            else launch_cop_ng<K, 32, 16>(d, col, nx, grid, st, end);
             break;
     }
 }
@@ -195,7 +208,7 @@ static void launch_direct_g(const V1Dev& d, int col, int nx, int grid, cudaStrea
 // Cop turn into column col (or, direct = 1, a deferred robber turn): every form that may apply
 // is enqueued; each reads the input frontier's row count on the device and only the matching
 // form does work.
-void launch_cop(const V1Dev& d, int col, int nx, int direct, int grid, cudaStream_t st) {
+void launch_cop(const V1Dev& d, int col, int nx, int direct, int grid, cudaStream_t st, bool end) {
     if (direct) {
         switch (group_lanes(d.g.rwp)) {
             case 4: launch_direct_g<4>(d, col, nx, grid, st); break;
@@ -206,10 +219,10 @@ void launch_cop(const V1Dev& d, int col, int nx, int direct, int grid, cudaStrea
         return;
     }
     switch (d.k) {
-        case 1: launch_cop_k<1>(d, col, nx, grid, st); break;
-        case 2: launch_cop_k<2>(d, col, nx, grid, st); break;
-        case 3: launch_cop_k<3>(d, col, nx, grid, st); break;
-        default: launch_cop_k<4>(d, col, nx, grid, st); break;
+        case 1: launch_cop_k<1>(d, col, nx, grid, st, end); break;
+        case 2: launch_cop_k<2>(d, col, nx, grid, st, end); break;
+        case 3: launch_cop_k<3>(d, col, nx, grid, st, end); break;
+        default: launch_cop_k<4>(d, col, nx, grid, st, end); break;
     }
 }
 

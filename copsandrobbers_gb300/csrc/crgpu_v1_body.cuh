@@ -147,23 +147,27 @@ struct Tally {
 // frontier already holds the capture seeds).  Before an odd column it also clears the candidate
 // rows of the push-mode cop turn just run.  Every block reads the column's state first; the
 // last block to finish (counted in sync[0]) resets it, so no block reads a half-reset state.
-__device__ CR_BODY_INLINE void prep_clear(const V1Dev& d, int col, unsigned wk, unsigned nwk) {
+__device__ CR_BODY_INLINE void prep_clear_flags(const V1Dev& d, int col, unsigned wk, unsigned nwk) {
     const ColMeta* mo = d.meta + col;
     if (!mo->append && !mo->clean) {
         uint8_t* f = d.fflag + (size_t)col * d.C;
         for (size_t i = (size_t)wk * blockDim.x + threadIdx.x; i < d.C; i += (size_t)nwk * blockDim.x)
             f[i] = 0;
     }
-    if (col % 2 == 1) {
-        // the candidate rows (and their bitmap words) the cop turn into column col - 1 consumed
-        const size_t words = (size_t)d.S * d.g.rwp, total = (size_t)d.sync[1] * words;
-        for (size_t i = (size_t)wk * blockDim.x + threadIdx.x; i < total; i += (size_t)nwk * blockDim.x) {
-            const uint32_t cid = d.clist[i / words];
-            const size_t e = i % words;
-            d.cand[(size_t)cid * words + e] = 0u;
-            if (e == 0) d.cbits[cid >> 5] = 0u;
-        }
+}
+// The candidate rows (and their bitmap words) the last push-mode cop turn consumed.
+__device__ CR_BODY_INLINE void prep_clear_cand(const V1Dev& d, unsigned wk, unsigned nwk) {
+    const size_t words = (size_t)d.S * d.g.rwp, total = (size_t)d.sync[1] * words;
+    for (size_t i = (size_t)wk * blockDim.x + threadIdx.x; i < total; i += (size_t)nwk * blockDim.x) {
+        const uint32_t cid = d.clist[i / words];
+        const size_t e = i % words;
+        d.cand[(size_t)cid * words + e] = 0u;
+        if (e == 0) d.cbits[cid >> 5] = 0u;
     }
+}
+__device__ CR_BODY_INLINE void prep_clear(const V1Dev& d, int col, unsigned wk, unsigned nwk) {
+    prep_clear_flags(d, col, wk, nwk);
+    if (col % 2 == 1) prep_clear_cand(d, wk, nwk);
 }
 
 // Thread 0 of each block of a grid (after the block's work and a __syncthreads): true in the

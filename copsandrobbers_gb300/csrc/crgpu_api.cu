@@ -662,16 +662,16 @@ static int v1_init(cr_solver* s, uint64_t* caps) {
 // initializeCaptures and pass 1 of a p = 1 solve in one kernel (init_pass1_single /
 // init_pass1_body): every table byte, both marked planes and both flag planes are written whole
 // (column 1's frontier rows where they gained marks), so nothing is cleared first.
-static int v1_init_pass1_enqueue(cr_solver* s) {
+static int v1_init_pass1_enqueue(cr_solver* s, bool defer_list = false) {
     cr_context* ctx = s->ctx;
     cudaStream_t st = ctx->stream;
     CR_CUDA(ctx, cudaMemsetAsync(s->d_counters, 0, 4 * sizeof(unsigned long long), st));
     CR_CUDA(ctx, cudaMemsetAsync(s->d_err, 0, sizeof(unsigned), st));
     // column 0's frontier after pass 1 is every row (the implicit list), already consumed by
     // the fused last column, which leaves its flags clear; column 1's list is built from its
-    // flags after the kernel
+    // flags after the kernel, by k_list_compact or (defer_list) by the pass loop's entry
     ColMeta meta[2] = {ColMeta{0, 0, 0, 0, (int)std::min<uint64_t>(s->C, INT32_MAX), 0, -1, 1},
-                       ColMeta{1, kEmptyLo, -1, 0, 0, 0, 0, 0}};
+                       ColMeta{1, kEmptyLo, -1, 0, 0, 0, 0, 0, 0, defer_list ? 1 : 0}};
     CR_CUDA(ctx, cudaMemsetAsync(s->d_sync, 0, 2 * sizeof(unsigned), st));
     CR_CUDA(ctx, cudaMemcpyAsync(s->d_meta, meta, sizeof(meta), cudaMemcpyHostToDevice, st));
     V1Dev d = dev_view(s);
@@ -679,10 +679,12 @@ static int v1_init_pass1_enqueue(cr_solver* s) {
     launch_init_pass1(d, ctx->num_sms, st);
     CR_CUDA(ctx, cudaGetLastError());
     CR_CUDA(ctx, cudaEventRecord(s->evc1, st));
-    launch_list_compact(d, 1, ctx->num_sms, st);   // column 1's row list, from its flags
-    CR_CUDA(ctx, cudaGetLastError());
+    if (!defer_list) {
+        launch_list_compact(d, 1, ctx->num_sms, st);   // column 1's row list, from its flags
+        CR_CUDA(ctx, cudaGetLastError());
+    }
     s->init_pending = false;
-    s->stats.kernel_launches += 2;
+    s->stats.kernel_launches += defer_list ? 1 : 2;
     return CR_OK;
 }
 
@@ -954,7 +956,7 @@ static int v1_run_on_device(cr_solver* s) {
     const bool first = s->init_pending;
     CR_CUDA(ctx, cudaEventRecord(s->ev0, st));
     if (first) {
-        if (int rc = v1_init_pass1_enqueue(s)) return rc;
+        if (int rc = v1_init_pass1_enqueue(s, true)) return rc;
     }
     CR_CUDA(ctx, cudaMemsetAsync(s->d_hist_n, 0, sizeof(int), st));
     if (first) CR_CUDA(ctx, cudaMemsetAsync(s->d_hist_n, 1, 1, st));   // the length 1 (low byte)

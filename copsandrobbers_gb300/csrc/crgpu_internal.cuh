@@ -47,6 +47,8 @@ struct ColMeta {
     // Largest value among the column's marks made before the current frontier's producer run
     // (captures, value 0, are always among them; value-initialised brace lists leave it 0).
     int old_hi;
+    // 1 = the list is still to be built from the flags (by the pass loop's entry kernel)
+    int compact;
 };
 
 // Candidate rows of the push-mode cop turn: a bitmap of C bits marks the configurations that

@@ -46,6 +46,8 @@ namespace crgpu {
 
 using namespace grid;
 
+__device__ void list_compact_body(const V1Dev& d, int col);
+
 __global__ void k_prep(V1Dev d, int col, int nx) { prep_body(d, col, nx, blockIdx.x, gridDim.x); }
 __global__ void k_init(V1Dev d, int K) { init_body(d, K, blockIdx.x, gridDim.x); }
 // The first pass in two instances: rows of one 256-robber block split into whole lane pieces
@@ -126,10 +128,14 @@ __global__ void __launch_bounds__(256, 4) k_and_end(V1Dev d, int col, LoopCtl c)
 // block records a first pass run just before the loop (*idx = 1, set by the host) as the
 // history's first entry and starts the loop if the last pass found something and no error bit
 // is set.
-__global__ void k_loop_enter(V1Dev d, LoopCtl c) {
+__global__ void __launch_bounds__(256) k_loop_enter(V1Dev d, LoopCtl c) {
+    // column 1's row list after a fused first pass (every block reads the marker before the
+    // last block clears it)
+    if (d.meta[1].compact) list_compact_body(d, 1);
     prep_clear(d, 0, blockIdx.x, gridDim.x);
     __syncthreads();
     if (threadIdx.x == 0 && grid_last_block(d, gridDim.x)) {
+        d.meta[1].compact = 0;
         const unsigned long long f = *d.pass_new;
         if (*c.idx == 1) c.hist[0] = f;
         cudaGraphSetConditional(c.loop, (f != 0ull && *d.err == 0u) ? 1u : 0u);
@@ -306,7 +312,7 @@ void launch_init_pass1(const V1Dev& d, int num_sms, cudaStream_t st) {
 // Builds column col's row list from its flag plane (after the first pass): each block takes
 // segments of 16 flags per thread, counts the set ones, reserves its segment's room in the list
 // with one atomic and writes the ids (the list order is irrelevant to its consumers).
-__global__ void __launch_bounds__(256) k_list_compact(V1Dev d, int col) {
+__device__ void list_compact_body(const V1Dev& d, int col) {
     __shared__ unsigned s_warp[8];
     __shared__ unsigned s_at;
     constexpr int kPer = 16;
@@ -349,6 +355,7 @@ __global__ void __launch_bounds__(256) k_list_compact(V1Dev d, int col) {
         __syncthreads();
     }
 }
+__global__ void __launch_bounds__(256) k_list_compact(V1Dev d, int col) { list_compact_body(d, col); }
 
 void launch_list_compact(const V1Dev& d, int col, int num_sms, cudaStream_t st) {
     const uint64_t segs = ((uint64_t)d.C + 256 * 16 - 1) / (256 * 16);

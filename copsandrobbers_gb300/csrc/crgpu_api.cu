@@ -62,6 +62,7 @@ struct cr_solver {
     std::vector<uint16_t> h_ccol;
     bool cop_stay = false, robber_stay = false;
     int cop_maxdeg = 0;
+    uint32_t forms = CR_FORMS_ALL;    // cr_solver_set_forms
     uint32_t* d_crp = nullptr;        // set only when the two move graphs differ
     uint16_t* d_ccol = nullptr;
     uint32_t* d_ciso = nullptr;
@@ -346,6 +347,12 @@ static V1Dev dev_view(const cr_solver* s) {
     d.cand = s->d_cand;
     d.h1 = s->d_h1;
     d.cbits = s->d_cbits;
+    // forms switched off: no pair rows (the tuple pull), a push ratio that always or never
+    // pushes, the last column's general form
+    if (!(s->forms & CR_FORM_SEPARABLE)) d.h1 = nullptr;
+    if (!(s->forms & CR_FORM_PULL)) d.push_ratio = 0u;
+    else if (!(s->forms & CR_FORM_PUSH)) d.push_ratio = 0xFFFFFFFFu;
+    d.fresh_last = (s->forms & CR_FORM_FRESH_LAST) ? 1 : 0;
     d.list = s->d_list;
     d.clist = s->d_clist;
     d.sync = s->d_sync;
@@ -774,7 +781,7 @@ static int v1_pass(cr_solver* s, uint64_t* found) {
     CR_CUDA(ctx, cudaStreamSynchronize(st));
     int per_pass = s->cols;  // prep kernels
     for (int col = 0; col < s->cols; ++col)
-        per_pass += col % 2 == 0 ? cop_launches_k(0, s->k, s->d_h1 != nullptr) : (col < s->cols - 1 ? cop_launches(1) : 1);
+        per_pass += col % 2 == 0 ? cop_launches_k(0, s->k, s->d_h1 != nullptr && (s->forms & CR_FORM_SEPARABLE)) : (col < s->cols - 1 ? cop_launches(1) : 1);
     s->stats.kernel_launches += per_pass;
     *found = s->h_pinned[0];
     return CR_OK;
@@ -787,7 +794,7 @@ int cr_solver_init(cr_solver* s, uint64_t* base_captures) {
     uint64_t caps = 0;
     s->init_pending = false;
     int rc = CR_OK;
-    if (s->rules == CR_RULES_V1 && s->cols == 2 && s->S >= 2 && s->cover_w > 0) {
+    if (s->rules == CR_RULES_V1 && s->cols == 2 && s->S >= 2 && s->cover_w > 0 && (s->forms & CR_FORM_FUSED_FIRST)) {
         // folded into pass 1; the capture count has a closed form: every configuration
         // contributes its distinct cop vertices, and n * (multisets containing a given vertex)
         // = n * (C(n+k-1, k) - C(n+k-2, k))
@@ -986,7 +993,7 @@ static int v1_run_on_device(cr_solver* s) {
     // column's in the cop turn and the last column
     int per_pass = s->cols == 2 ? 0 : s->cols - 1;
     for (int col = 0; col < s->cols; ++col)
-        per_pass += col % 2 == 0 ? cop_launches_k(0, s->k, s->d_h1 != nullptr) : (col < s->cols - 1 ? cop_launches(1) : 1);
+        per_pass += col % 2 == 0 ? cop_launches_k(0, s->k, s->d_h1 != nullptr && (s->forms & CR_FORM_SEPARABLE)) : (col < s->cols - 1 ? cop_launches(1) : 1);
     s->stats.kernel_launches += (int64_t)per_pass * loop_passes + 1;   // and the loop's entry
     if (bits & kErrRank) return fail(ctx, CR_ERR_INTERNAL, "successor rank out of range");
     if (bits & kErrSlot) {
@@ -1080,6 +1087,22 @@ int cr_solver_stats(cr_solver* s, cr_solve_stats* out) {
 int cr_solver_v2_hash_stats(cr_solver* s, cr_v2_hash_stats* out) {
     if (!s || !out) return CR_ERR_INVALID;
     *out = s->v2 ? crgpu::v2_hash_stats(s->v2) : cr_v2_hash_stats{};
+    return CR_OK;
+}
+
+int cr_solver_set_forms(cr_solver* s, uint32_t mask) {
+    if (!s) return CR_ERR_INVALID;
+    if ((mask & ~CR_FORMS_ALL) || !(mask & (CR_FORM_PUSH | CR_FORM_PULL)))
+        return fail(s->ctx, CR_ERR_INVALID, "forms: mask 0x%x (unknown bits, or neither push nor pull)", mask);
+    if (s->rules != CR_RULES_V1 && mask != CR_FORMS_ALL)
+        return fail(s->ctx, CR_ERR_INVALID, "forms: v2 solves have one form");
+    if (mask == s->forms) return CR_OK;
+    s->forms = mask;
+    // the captured pass graphs hold the old device view
+    if (s->pass_graph) cudaGraphExecDestroy(s->pass_graph);
+    s->pass_graph = nullptr;
+    if (s->run_graph) cudaGraphExecDestroy(s->run_graph);
+    s->run_graph = nullptr;
     return CR_OK;
 }
 

@@ -97,6 +97,9 @@ struct V1Dev {
     // stage the graph arrays its row tests read (0 = none)
     uint32_t and_stage_words = 0;
     uint32_t C;
+    // a frontier with rows * push_ratio < C is pushed (kPushRatio; 0 = always push, ~0 = never)
+    uint32_t push_ratio = kPushRatio;
+    int fresh_last = 1;       // 0 = the last column always takes its general form
     const uint32_t* binom;    // [k][n + 1]: B[i][x] = C(n - x + k - 1 - i, k - i)
     const uint16_t* configs;  // [C][k]
     const uint32_t* hop;      // [n][rwp]: vertices exactly p robber moves from r

@@ -51,8 +51,8 @@ __host__ __device__ inline int rank_table_words(int k, int n) { return (k * (n +
 // Words of shared memory the separable turn's pair rows stage frontier rows in (16 KB).
 constexpr int kPairStageWords = 4096;
 
-__device__ __forceinline__ bool frontier_sparse(const ColMeta& m, uint32_t C) {
-    return (unsigned long long)m.rows * kPushRatio < C;
+__device__ __forceinline__ bool frontier_sparse(const V1Dev& d, const ColMeta& m) {
+    return (unsigned long long)m.rows * d.push_ratio < d.C;
 }
 
 // A warp's buffer of row ids bound for a column's list: up to 32 ids, one per lane, written out
@@ -1005,7 +1005,7 @@ __device__ CR_BODY_INLINE void cop_pull_body(const V1Dev& d, int col, int nx, un
     const int n = d.g.n, rw = d.g.rw, rwp = d.g.rwp, S = d.S;
     const ColMeta mi = d.meta[nx];
     if (mi.hi < mi.lo) return;                              // empty frontier: nothing changes
-    if (mi.seed || frontier_sparse(mi, d.C)) return;       // the seed or push form handles it
+    if (mi.seed || frontier_sparse(d, mi)) return;       // the seed or push form handles it
     if (K == 3 && d.h1) return;                             // the separable form handles it
     const int base_in = mi.base;
     const int s_used = min(mi.hi - base_in + 1, S);
@@ -1193,7 +1193,7 @@ __device__ CR_BODY_INLINE void pair_h1_body(const V1Dev& d, int nx, unsigned wk,
     constexpr int K = 3;
     const int n = d.g.n, rwp = d.g.rwp, S = d.S;
     const ColMeta mi = d.meta[nx];
-    if (!d.h1 || mi.hi < mi.lo || mi.seed || frontier_sparse(mi, d.C)) return;
+    if (!d.h1 || mi.hi < mi.lo || mi.seed || frontier_sparse(d, mi)) return;
     const int s_used = min(mi.hi - mi.base + 1, S);
     const int nwords = s_used * rwp;
     const int np1 = n + 1;
@@ -1293,7 +1293,7 @@ __device__ CR_BODY_INLINE void sep_pull_body(const V1Dev& d, int col, int nx, un
     const int gl = L.glane;
     const int n = d.g.n, rw = d.g.rw, rwp = d.g.rwp, S = d.S;
     const ColMeta mi = d.meta[nx];
-    if (!d.h1 || mi.hi < mi.lo || mi.seed || frontier_sparse(mi, d.C)) return;
+    if (!d.h1 || mi.hi < mi.lo || mi.seed || frontier_sparse(d, mi)) return;
     const int base_in = mi.base;
     const int s_used = min(mi.hi - base_in + 1, S);
     const int nwords = s_used * rwp;
@@ -1425,7 +1425,7 @@ __device__ CR_BODY_INLINE void cop_push_body(const V1Dev& d, int col, int nx, un
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int n = d.g.n, rwp = d.g.rwp, S = d.S;
     const ColMeta mi = d.meta[nx];
-    if (mi.seed || !frontier_sparse(mi, d.C)) return;           // a dense form takes this frontier
+    if (mi.seed || !frontier_sparse(d, mi)) return;           // a dense form takes this frontier
     if (wk == 0 && threadIdx.x == 0) d.meta[nx].clean = 1;   // every listed flag is cleared below
     if (mi.hi < mi.lo) return;
     const int s_used = min(mi.hi - mi.base + 1, S);
@@ -1515,7 +1515,7 @@ __device__ CR_BODY_INLINE void cop_apply_body(const V1Dev& d, int col, int nx, u
     const int gl = L.glane;
     const int rw = d.g.rw, rwp = d.g.rwp, S = d.S;
     const ColMeta mi = d.meta[nx];
-    if (mi.hi < mi.lo || mi.seed || !frontier_sparse(mi, d.C)) return;
+    if (mi.hi < mi.lo || mi.seed || !frontier_sparse(d, mi)) return;
     const int base_in = mi.base;
     const int s_used = min(mi.hi - base_in + 1, S);
     const int out_base = d.meta[col].base;
@@ -1647,7 +1647,7 @@ __device__ CR_BODY_INLINE void and_body(const V1Dev& d, int col, unsigned wk, un
     }
     const int avg_deg = max(1, (nnz + n - 1) / n);
     const int slo = mi.lo - mi.base, shi = mi.hi - mi.base;
-    const bool fresh = mi.old_hi <= mi.lo && slo >= 0 && shi < S;
+    const bool fresh = d.fresh_last && mi.old_hi <= mi.lo && slo >= 0 && shi < S;
     Tally t;
     for (uint32_t b0 = (wk * (blockDim.x >> 5) + warp) * CPW; b0 < rl.n; b0 += step) {
         {

@@ -19,6 +19,13 @@ ERRORS = {
 CR_RULES_V1 = 1
 CR_RULES_V2 = 2
 CR_COP_STAY = 0x10
+# kernel forms of a v1 solve (cr_solver_set_forms)
+CR_FORM_FUSED_FIRST = 0x01
+CR_FORM_PUSH = 0x02
+CR_FORM_PULL = 0x04
+CR_FORM_SEPARABLE = 0x08
+CR_FORM_FRESH_LAST = 0x10
+CR_FORMS_ALL = 0x1F
 CR_ROBBER_STAY = 0x20
 CR_MAX_K = 4
 
@@ -124,6 +131,7 @@ SIGNATURES = {
     "cr_solver_load_table_file": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
     "cr_solver_v2_hash_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(CrV2HashStats)]),
     "cr_solver_set_v2_hash_capacity": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
+    "cr_solver_set_forms": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32]),
     "cr_solver_perfect_game": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64),
                                               ctypes.POINTER(ctypes.c_int32), ctypes.c_int32,
                                               ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),

@@ -137,6 +137,11 @@ class Solver:
         _check(self.ctx.ptr, N.lib().cr_solver_v2_hash_stats(self.ptr, ctypes.byref(s)))
         return s
 
+    def set_forms(self, mask: int) -> None:
+        """Restrict a v1 solve to a subset of its kernel forms (N.CR_FORM_*); the results do
+        not depend on the mask."""
+        _check(self.ctx.ptr, N.lib().cr_solver_set_forms(self.ptr, mask))
+
     def set_v2_hash_capacity(self, slots: int) -> None:
         """Resize the v2 cloud table (0 = none); results do not depend on its size."""
         _check(self.ctx.ptr, N.lib().cr_solver_set_v2_hash_capacity(self.ptr, slots))

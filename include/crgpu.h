@@ -183,6 +183,19 @@ int cr_solver_v2_hash_stats(cr_solver* s, cr_v2_hash_stats* out);
  * default is twice the depth-1 nodes, capped at 2^24 slots.  Call between passes only. */
 int cr_solver_set_v2_hash_capacity(cr_solver* s, uint64_t slots);
 
+/* Kernel forms a v1 solve may choose from (all by default).  The forms are alternative ways to
+ * compute the same pass, so the tables, pass counts and verdicts never depend on the mask; it
+ * exists to test and compare each form.  No counterpart in the reference (its solver has one
+ * sweep).  CR_FORM_PUSH and CR_FORM_PULL cannot both be off.  Takes effect from the next pass
+ * (CR_FORM_FUSED_FIRST from the next cr_solver_init).  v2 solves accept CR_FORMS_ALL only. */
+#define CR_FORM_FUSED_FIRST 0x01u  /* initializeCaptures and pass 1 in one kernel (p = 1) */
+#define CR_FORM_PUSH        0x02u  /* cop turns of sparse frontiers: scatter to predecessors */
+#define CR_FORM_PULL        0x04u  /* cop turns of dense frontiers: gather from successors */
+#define CR_FORM_SEPARABLE   0x08u  /* the dense cop turn through pair rows (k = 3) */
+#define CR_FORM_FRESH_LAST  0x10u  /* the last column from this pass's column-0 marks */
+#define CR_FORMS_ALL        0x1Fu
+int cr_solver_set_forms(cr_solver* s, uint32_t mask);
+
 /* ---- whole solves ---------------------------------------------------------------------- */
 
 /* loadGraphFile..findFinalResult in one call.  states_out (host, may be NULL) receives the
